@@ -1,0 +1,126 @@
+"""ctypes mirror of include/euc_gb300.h (structs, enums, constants).
+
+Field order and types match the C header exactly; `tests/test_abi.py` checks
+the struct sizes against the C compiler's.
+"""
+import ctypes as C
+
+ABI_VERSION = 1
+
+# status codes
+OK = 0
+ERR_INVALID = 1
+ERR_SIZE_MISMATCH = 2
+ERR_INDEX_OOB = 3
+ERR_OOM = 4
+ERR_CUDA = 5
+ERR_BAND = 6
+ERR_TIMEOUT = 7
+ERR_BUDGET = 8
+ERR_CAPACITY = 9
+
+STATUS_NAMES = {
+    OK: "EUC_OK", ERR_INVALID: "EUC_ERR_INVALID", ERR_SIZE_MISMATCH: "EUC_ERR_SIZE_MISMATCH",
+    ERR_INDEX_OOB: "EUC_ERR_INDEX_OOB", ERR_OOM: "EUC_ERR_OOM", ERR_CUDA: "EUC_ERR_CUDA",
+    ERR_BAND: "EUC_ERR_BAND", ERR_TIMEOUT: "EUC_ERR_TIMEOUT", ERR_BUDGET: "EUC_ERR_BUDGET",
+    ERR_CAPACITY: "EUC_ERR_CAPACITY",
+}
+
+TEST_NONE, TEST_LESS, TEST_EQUAL, TEST_GREATER = 0, 1, 2, 3
+CULL_NONE, CULL_BACK, CULL_FRONT = 0, 1, 2
+Y_DOWN, Y_UP = 0, 1
+LEFT, RIGHT = 0, 1
+FMT_NONE, FMT_RGBA8, FMT_BGRA8, FMT_RGB8, FMT_R32F = 0, 1, 2, 3, 4
+SHADER_FLAT, SHADER_VCOLOR, SHADER_GOURAUD, SHADER_TEXTURED, SHADER_PHONG, SHADER_SHADOW = range(6)
+BLEND_REPLACE, BLEND_ALPHA = 0, 1
+FILTER_NEAREST, FILTER_LINEAR = 0, 1
+WRAP_NONE, WRAP_CLAMP, WRAP_TILE, WRAP_MIRROR = 0, 1, 2, 3
+BANDS_PAR = 0
+BANDS_SEQ = 0xFFFFFFFF
+FLAG_PAR_EMPTY = 1
+
+FMT_BPP = {FMT_NONE: 0, FMT_RGBA8: 4, FMT_BGRA8: 4, FMT_RGB8: 3, FMT_R32F: 4}
+
+
+class PipelineDesc(C.Structure):
+    _fields_ = [
+        ("shader", C.c_uint32), ("pixel_write", C.c_uint32), ("depth_test", C.c_uint32),
+        ("depth_write", C.c_uint32), ("handedness", C.c_uint32), ("y_axis", C.c_uint32),
+        ("z_clip", C.c_uint32), ("z_clip_min", C.c_float), ("z_clip_max", C.c_float),
+        ("aa_level", C.c_uint32), ("cull", C.c_uint32), ("blend", C.c_uint32),
+        ("band_rows", C.c_uint32), ("flags", C.c_uint32),
+    ]
+
+
+class Target(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("pitch", C.c_uint32), ("format", C.c_uint32)]
+
+
+class Sampler(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("pitch", C.c_uint32), ("format", C.c_uint32), ("filter", C.c_uint32),
+                ("wrap", C.c_uint32), ("texel_div", C.c_float), ("reserved", C.c_uint32)]
+
+
+class VertexLayout(C.Structure):
+    _fields_ = [("stride", C.c_uint32), ("position", C.c_int32), ("normal", C.c_int32),
+                ("uv", C.c_int32), ("color", C.c_int32)]
+
+
+Mat4 = C.c_float * 16
+
+
+class FlatUniforms(C.Structure):
+    _fields_ = [("mvp", Mat4), ("color", C.c_float * 4)]
+
+
+class VColorUniforms(C.Structure):
+    _fields_ = [("mvp", Mat4)]
+
+
+class GouraudUniforms(C.Structure):
+    _fields_ = [("mvp", Mat4), ("model", Mat4), ("to_light", C.c_float * 3), ("ambient", C.c_float),
+                ("color", C.c_float * 3), ("diffuse", C.c_float)]
+
+
+class TexturedUniforms(C.Structure):
+    _fields_ = [("mvp", Mat4), ("tex", Sampler)]
+
+
+class PhongUniforms(C.Structure):
+    _fields_ = [("model", Mat4), ("view", Mat4), ("proj", Mat4), ("light_vp", Mat4),
+                ("light_pos", C.c_float * 3), ("normal_sign", C.c_float), ("cam_pos", C.c_float * 3),
+                ("ambient", C.c_float), ("surf_color", C.c_float * 4), ("tex", Sampler),
+                ("shadow", Sampler)]
+
+
+class ShadowUniforms(C.Structure):
+    _fields_ = [("mvp", Mat4)]
+
+
+UNIFORMS_FOR_SHADER = {
+    SHADER_FLAT: FlatUniforms, SHADER_VCOLOR: VColorUniforms, SHADER_GOURAUD: GouraudUniforms,
+    SHADER_TEXTURED: TexturedUniforms, SHADER_PHONG: PhongUniforms, SHADER_SHADOW: ShadowUniforms,
+}
+
+
+class Stats(C.Structure):
+    _fields_ = [("triangles", C.c_uint64), ("culled", C.c_uint64), ("candidates", C.c_uint64)]
+
+
+class Scene(C.Structure):
+    _fields_ = [("desc", PipelineDesc), ("layout", VertexLayout), ("vertices", C.c_void_p),
+                ("nverts", C.c_uint64), ("indices", C.c_void_p), ("nindices", C.c_uint64),
+                ("pixel", Target), ("depth", Target), ("uniforms", C.c_void_p),
+                ("uniforms_size", C.c_uint64)]
+
+
+def mat4(values):
+    """Row-major float[16] from any 4x4 array-like."""
+    flat = [float(v) for row in values for v in row] if hasattr(values[0], "__len__") else [float(v) for v in values]
+    return Mat4(*flat)
+
+
+def status_name(code):
+    return STATUS_NAMES.get(code, "EUC_STATUS_%d" % code)

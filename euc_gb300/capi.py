@@ -1,0 +1,120 @@
+"""ctypes binding of libeuc_gb300.so (the C ABI in include/euc_gb300.h).
+
+There is no fallback: if the library is missing or a call fails, this module
+raises.  The library is built by `python -m euc_gb300.build`.
+"""
+import ctypes as C
+import os
+
+from . import abi
+from . import build as _build
+
+_lib = None
+
+# every function that include/euc_gb300.h declares, with (restype, argtypes)
+SIGNATURES = {
+    "euc_abi_version": (C.c_int, []),
+    "euc_status_string": (C.c_char_p, [C.c_int]),
+    "euc_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    "euc_ctx_destroy": (C.c_int, [C.c_void_p]),
+    "euc_ctx_reserve": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64]),
+    "euc_ctx_sync": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "euc_ctx_stats": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(abi.Stats)]),
+    "euc_render": (C.c_int, [C.c_void_p, C.POINTER(abi.PipelineDesc), C.c_void_p, C.c_size_t,
+                             C.POINTER(abi.VertexLayout), C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
+                             C.POINTER(abi.Target), C.POINTER(abi.Target), C.c_void_p]),
+    "euc_render_host": (C.c_int, [C.c_void_p, C.POINTER(abi.PipelineDesc), C.c_void_p, C.c_size_t,
+                                  C.POINTER(abi.VertexLayout), C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
+                                  C.POINTER(abi.Target), C.POINTER(abi.Target)]),
+    "euc_render_batch": (C.c_int, [C.c_void_p, C.POINTER(abi.Scene), C.c_size_t, C.c_void_p]),
+}
+
+
+class EucError(RuntimeError):
+    def __init__(self, code, what=""):
+        self.code = code
+        super().__init__("%s%s (%s)" % (what + ": " if what else "", abi.status_name(code), status_string(code)))
+
+
+def lib_path():
+    return _build.LIB
+
+
+def lib():
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        path = lib_path()
+        if not os.path.exists(path):
+            raise RuntimeError("libeuc_gb300.so is not built (%s); run `python -m euc_gb300.build`" % path)
+        L = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        if L.euc_abi_version() != abi.ABI_VERSION:
+            raise RuntimeError("ABI version mismatch: library %d, bindings %d" % (L.euc_abi_version(), abi.ABI_VERSION))
+        _lib = L
+    return _lib
+
+
+def status_string(code):
+    try:
+        return lib().euc_status_string(code).decode()
+    except Exception:  # the library may be what failed to load
+        return abi.status_name(code)
+
+
+def check(code, what=""):
+    if code != abi.OK:
+        raise EucError(code, what)
+    return code
+
+
+class Context:
+    """Owns an euc_ctx (scratch buffers, staging ring) on one CUDA device."""
+
+    def __init__(self, device=0):
+        self.device = device
+        h = C.c_void_p()
+        check(lib().euc_ctx_create(device, C.byref(h)), "euc_ctx_create")
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            lib().euc_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reserve(self, max_verts, max_tris, max_pixels, max_scenes=1):
+        check(lib().euc_ctx_reserve(self.handle, max_verts, max_tris, max_pixels, max_scenes), "euc_ctx_reserve")
+
+    def sync(self, stream=None):
+        return lib().euc_ctx_sync(self.handle, stream)
+
+    def stats(self, stream=None):
+        s = abi.Stats()
+        check(lib().euc_ctx_stats(self.handle, stream, C.byref(s)), "euc_ctx_stats")
+        return s
+
+    def render(self, desc, uniforms, layout, vertices_ptr, nverts, indices_ptr, nindices, pixel, depth, stream=None):
+        """Raw euc_render: device pointers; returns the status code."""
+        return lib().euc_render(self.handle, C.byref(desc), C.addressof(uniforms), C.sizeof(uniforms),
+                                C.byref(layout), vertices_ptr, nverts, indices_ptr, nindices,
+                                C.byref(pixel) if pixel is not None else None,
+                                C.byref(depth) if depth is not None else None, stream)
+
+    def render_host(self, desc, uniforms, layout, vertices_ptr, nverts, indices_ptr, nindices, pixel, depth):
+        return lib().euc_render_host(self.handle, C.byref(desc), C.addressof(uniforms), C.sizeof(uniforms),
+                                     C.byref(layout), vertices_ptr, nverts, indices_ptr, nindices,
+                                     C.byref(pixel) if pixel is not None else None,
+                                     C.byref(depth) if depth is not None else None)
+
+    def render_batch(self, scenes, stream=None):
+        arr = (abi.Scene * len(scenes))(*scenes)
+        return lib().euc_render_batch(self.handle, arr, len(scenes), stream)

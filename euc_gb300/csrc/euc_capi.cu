@@ -1,0 +1,639 @@
+// euc_capi.cu — host runtime and C ABI of the GB300 triangle pipeline.
+//
+// A render is a batch of one scene; a batch runs every scene through the same
+// six launches (vertex per shader kind, setup, scan, init, raster, resolve per
+// shader kind) on one stream.  Scratch buffers live in the context and grow
+// on demand (euc_ctx_reserve pre-sizes them).  Scene tables and uniforms go
+// up through a ring of pinned staging slots, each guarded by an event.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "euc_kernels.cuh"
+
+using namespace eucg;
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+};
+
+constexpr int kStageSlots = 8;
+
+struct StageSlot {
+    void *host = nullptr;
+    void *dev = nullptr;
+    size_t cap = 0;
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+};
+
+}  // namespace
+
+struct euc_ctx {
+    int device = 0;
+    int nsm = 0;
+    DevBuf clip, vdata, recs, rows, chunk_sums, live_tri, live_rowoff, totals, vbuf, err, stats;
+    // buffers used by euc_render_host
+    DevBuf h_verts, h_idx, h_pixel, h_depth, h_tex[2];
+    StageSlot slots[kStageSlots];
+    int next_slot = 0;
+    int last_nscenes = 0;
+    std::mutex mu;
+};
+
+namespace {
+
+#define CUDA_TRY(x)                                  \
+    do {                                             \
+        cudaError_t e_ = (x);                        \
+        if (e_ != cudaSuccess) {                     \
+            (void)cudaGetLastError();                \
+            return e_ == cudaErrorMemoryAllocation ? EUC_ERR_OOM : EUC_ERR_CUDA; \
+        }                                            \
+    } while (0)
+
+int grow(DevBuf &b, size_t bytes) {
+    if (bytes <= b.cap) return EUC_OK;
+    size_t ncap = std::max(bytes, b.cap + b.cap / 2);
+    ncap = (ncap + 255) & ~(size_t)255;
+    if (b.p) {
+        CUDA_TRY(cudaDeviceSynchronize());
+        CUDA_TRY(cudaFree(b.p));
+        b.p = nullptr;
+        b.cap = 0;
+    }
+    CUDA_TRY(cudaMalloc(&b.p, ncap));
+    b.cap = ncap;
+    return EUC_OK;
+}
+
+inline uint64_t pad_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
+
+uint32_t fmt_bpp(uint32_t f) {
+    switch (f) {
+    case EUC_FMT_RGBA8: case EUC_FMT_BGRA8: case EUC_FMT_R32F: return 4;
+    case EUC_FMT_RGB8: return 3;
+    default: return 0;
+    }
+}
+
+size_t uniforms_size_for(uint32_t shader) {
+    switch (shader) {
+    case EUC_SHADER_FLAT: return sizeof(euc_flat_uniforms);
+    case EUC_SHADER_VCOLOR: return sizeof(euc_vcolor_uniforms);
+    case EUC_SHADER_GOURAUD: return sizeof(euc_gouraud_uniforms);
+    case EUC_SHADER_TEXTURED: return sizeof(euc_textured_uniforms);
+    case EUC_SHADER_PHONG: return sizeof(euc_phong_uniforms);
+    case EUC_SHADER_SHADOW: return sizeof(euc_shadow_uniforms);
+    default: return 0;
+    }
+}
+
+int shader_nv(uint32_t shader) {
+    switch (shader) {
+    case EUC_SHADER_FLAT: return FlatFn::NV;
+    case EUC_SHADER_VCOLOR: return VColorFn::NV;
+    case EUC_SHADER_GOURAUD: return GouraudFn::NV;
+    case EUC_SHADER_TEXTURED: return TexturedFn::NV;
+    case EUC_SHADER_PHONG: return PhongFn::NV;
+    case EUC_SHADER_SHADOW: return ShadowFn::NV;
+    default: return 0;
+    }
+}
+
+bool attr_ok(int32_t off, uint32_t bytes, uint32_t stride) {
+    return off >= 0 && (off & 3) == 0 && (uint32_t)off + bytes <= stride;
+}
+
+int check_sampler(const euc_sampler &s) {
+    if (!s.data) return EUC_OK;
+    // euc's `Texture::linear()` asserts a non-empty texture (texture.rs:63-66).
+    if (s.width < 1 || s.height < 1) return EUC_ERR_INVALID;
+    if (s.format != EUC_FMT_RGBA8 && s.format != EUC_FMT_R32F) return EUC_ERR_INVALID;
+    if (s.filter > EUC_FILTER_LINEAR || s.wrap > EUC_WRAP_MIRROR) return EUC_ERR_INVALID;
+    if ((s.pitch & 3) || (s.pitch && s.pitch < s.width * 4)) return EUC_ERR_INVALID;
+    if (((uintptr_t)s.data & 3) != 0) return EUC_ERR_INVALID;
+    if (s.format == EUC_FMT_RGBA8 && !(s.texel_div > 0.0f)) return EUC_ERR_INVALID;
+    return EUC_OK;
+}
+
+// Host-side plan of one scene.
+struct Plan {
+    SceneDev d;
+    bool skip;       // nothing observable is drawn
+    uint32_t nv;     // VertexData floats
+    const void *uniforms;
+    size_t usize;
+};
+
+// Validates a scene and fills its plan (everything but the batch offsets).
+// Mirrors euc's panics: target sizes (pipeline.rs:256-270), band height
+// (pipeline.rs:328-330).  Index bounds are checked on the device.
+int plan_scene(const euc_scene &sc, Plan &p) {
+    std::memset(&p, 0, sizeof(p));
+    const euc_pipeline_desc &d = sc.desc;
+    if (d.shader >= EUC_SHADER_COUNT) return EUC_ERR_INVALID;
+    if (d.depth_test > EUC_TEST_GREATER || d.cull > EUC_CULL_FRONT || d.y_axis > EUC_Y_UP) return EUC_ERR_INVALID;
+    if (d.blend != EUC_BLEND_REPLACE) return EUC_ERR_INVALID;  // order-dependent blends: not in this path
+    const size_t need = uniforms_size_for(d.shader);
+    if (!sc.uniforms || sc.uniforms_size < need) return EUC_ERR_INVALID;
+    const euc_vertex_layout &l = sc.layout;
+    if (l.stride == 0 || (l.stride & 3)) return EUC_ERR_INVALID;
+    if (sc.nverts && (!sc.vertices || ((uintptr_t)sc.vertices & 3))) return EUC_ERR_INVALID;
+    if (sc.indices && ((uintptr_t)sc.indices & 3)) return EUC_ERR_INVALID;
+    bool ok = true;
+    switch (d.shader) {
+    case EUC_SHADER_VCOLOR: ok = attr_ok(l.position, 16, l.stride) && attr_ok(l.color, 4, l.stride); break;
+    case EUC_SHADER_GOURAUD: ok = attr_ok(l.position, 12, l.stride) && attr_ok(l.normal, 12, l.stride); break;
+    case EUC_SHADER_TEXTURED: ok = attr_ok(l.position, 12, l.stride) && attr_ok(l.uv, 8, l.stride); break;
+    case EUC_SHADER_PHONG:
+        ok = attr_ok(l.position, 12, l.stride) && attr_ok(l.normal, 12, l.stride) && (l.uv < 0 || attr_ok(l.uv, 8, l.stride));
+        break;
+    default: ok = attr_ok(l.position, 12, l.stride); break;
+    }
+    if (!ok) return EUC_ERR_INVALID;
+    if (d.shader == EUC_SHADER_TEXTURED) {
+        const euc_textured_uniforms *u = (const euc_textured_uniforms *)sc.uniforms;
+        if (!u->tex.data) return EUC_ERR_INVALID;
+        if (int rc = check_sampler(u->tex)) return rc;
+    }
+    if (d.shader == EUC_SHADER_PHONG) {
+        const euc_phong_uniforms *u = (const euc_phong_uniforms *)sc.uniforms;
+        if (int rc = check_sampler(u->tex)) return rc;
+        if (int rc = check_sampler(u->shadow)) return rc;
+    }
+    const bool uses_depth = d.depth_test != EUC_TEST_NONE || d.depth_write;
+    const euc_target &px = sc.pixel, &dp = sc.depth;
+    const bool px_empty = px.data == nullptr, dp_empty = dp.data == nullptr;
+    if (!px_empty && d.pixel_write) {
+        const uint32_t bpp = fmt_bpp(px.format);
+        if (bpp == 0 || px.format == EUC_FMT_R32F) return EUC_ERR_INVALID;
+        const uint32_t pitch = px.pitch ? px.pitch : px.width * bpp;
+        if (pitch < px.width * bpp) return EUC_ERR_INVALID;
+        if (bpp == 4 && ((pitch & 3) || ((uintptr_t)px.data & 3))) return EUC_ERR_INVALID;
+    }
+    if (!dp_empty && uses_depth) {
+        if (dp.format != EUC_FMT_R32F) return EUC_ERR_INVALID;
+        const uint32_t pitch = dp.pitch ? dp.pitch : dp.width * 4;
+        if (pitch < dp.width * 4 || (pitch & 3) || ((uintptr_t)dp.data & 3)) return EUC_ERR_INVALID;
+    }
+    const uint32_t pw = px_empty ? 0 : px.width, ph = px_empty ? 0 : px.height;
+    const uint32_t dw = dp_empty ? 0 : dp.width, dh = dp_empty ? 0 : dp.height;
+    p.skip = false;
+    uint32_t W, H;
+    if (!d.pixel_write && !uses_depth) { p.skip = true; return EUC_OK; }  // pipeline.rs:257
+    if (d.pixel_write && !uses_depth) { W = pw; H = ph; }
+    else if (!d.pixel_write) { W = dw; H = dh; }
+    else {
+        if (pw != dw || ph != dh) return EUC_ERR_SIZE_MISMATCH;
+        W = pw; H = ph;
+    }
+    const uint32_t level = d.aa_level > 6 ? 6 : d.aa_level;
+    uint64_t gr;
+    if (d.band_rows == EUC_BANDS_PAR) {
+        gr = 20000ull * (1ull << level) / (W > 1 ? W : 1);
+        if (gr == 0) return EUC_ERR_BAND;
+        if (H / gr == 0) {
+            if (d.flags & EUC_FLAG_PAR_EMPTY) { p.skip = true; return EUC_OK; }
+            gr = H > 0 ? H : 1;
+        }
+    } else {
+        gr = d.band_rows;
+        if (gr > H) gr = H > 0 ? H : 1;
+    }
+    if (W == 0 || H == 0) { p.skip = true; return EUC_OK; }
+    const uint64_t nstream = sc.indices ? sc.nindices : sc.nverts;
+    if (sc.nverts >= 0xFFFFFFFFull || nstream / 3 >= 0x3FFFFFFFull) return EUC_ERR_INVALID;
+    SceneDev &s = p.d;
+    s.verts = (const uint8_t *)sc.vertices;
+    s.idx = sc.indices;
+    s.pixel = (uint8_t *)px.data;
+    s.depth = (uint8_t *)dp.data;
+    s.nverts = sc.nverts;
+    s.nstream = nstream;
+    s.lay = l;
+    s.ntris = (uint32_t)(nstream / 3);
+    s.ngroups = (uint32_t)((nstream + 2) / 3);
+    s.W = W;
+    s.H = H;
+    s.gr = (uint32_t)gr;
+    s.level = level;
+    s.ppitch = px_empty ? 0 : (px.pitch ? px.pitch : px.width * fmt_bpp(px.format));
+    s.dpitch = dp_empty ? 0 : (dp.pitch ? dp.pitch : dp.width * 4);
+    s.pfmt = px_empty ? EUC_FMT_NONE : px.format;
+    s.pixel_write = d.pixel_write ? 1 : 0;
+    s.depth_test = d.depth_test;
+    s.depth_write = d.depth_write ? 1 : 0;
+    s.yflip = d.y_axis == EUC_Y_UP ? 1 : 0;
+    s.zclip = d.z_clip ? 1 : 0;
+    s.zmin = d.z_clip_min;
+    s.zmax = d.z_clip_max;
+    s.cull = d.cull;
+    s.blend = d.blend;
+    s.shader = d.shader;
+    if (!s.pixel_write && !s.depth_write) { p.skip = true; return EUC_OK; }  // nothing is ever written
+    if (s.pixel_write && px_empty) s.pixel_write = 0;  // Empty drops writes (texture.rs:315-318)
+    s.keytype = (s.depth_write && (d.depth_test == EUC_TEST_LESS || d.depth_test == EUC_TEST_GREATER)) ? KEY_MIN : KEY_LAST;
+    p.nv = (uint32_t)shader_nv(d.shader);
+    p.uniforms = sc.uniforms;
+    p.usize = need;
+    return EUC_OK;
+}
+
+int acquire_slot(euc_ctx *ctx, size_t bytes, StageSlot *&out) {
+    StageSlot &s = ctx->slots[ctx->next_slot];
+    ctx->next_slot = (ctx->next_slot + 1) % kStageSlots;
+    if (s.pending) {
+        CUDA_TRY(cudaEventSynchronize(s.done));
+        s.pending = false;
+    }
+    if (s.cap < bytes) {
+        size_t ncap = std::max(bytes, (size_t)65536);
+        if (s.host) CUDA_TRY(cudaFreeHost(s.host));
+        if (s.dev) CUDA_TRY(cudaFree(s.dev));
+        s.host = s.dev = nullptr;
+        s.cap = 0;
+        CUDA_TRY(cudaMallocHost(&s.host, ncap));
+        CUDA_TRY(cudaMalloc(&s.dev, ncap));
+        s.cap = ncap;
+    }
+    if (!s.done) CUDA_TRY(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
+    out = &s;
+    return EUC_OK;
+}
+
+template <class F>
+void launch_vertex(const SceneDev *sc, const uint64_t *vb, int s0, int s1, uint64_t blk0, uint64_t nblk, euc_ctx *ctx,
+                   cudaStream_t st) {
+    if (nblk) k_vertex<F><<<(unsigned)nblk, kBlock, 0, st>>>(sc, vb, s0, s1, blk0, (float4 *)ctx->clip.p, (float *)ctx->vdata.p);
+}
+
+template <class F>
+void launch_resolve(const SceneDev *sc, const uint64_t *pb, int s0, int s1, uint64_t blk0, uint64_t nblk, euc_ctx *ctx,
+                    cudaStream_t st) {
+    if (nblk)
+        k_resolve<F><<<(unsigned)nblk, kBlock, 0, st>>>(sc, pb, s0, s1, blk0, (const TriRec *)ctx->recs.p,
+                                                        (const float *)ctx->vdata.p, (const unsigned long long *)ctx->vbuf.p);
+}
+
+void dispatch_vertex(uint32_t shader, const SceneDev *sc, const uint64_t *vb, int s0, int s1, uint64_t blk0, uint64_t nblk,
+                     euc_ctx *ctx, cudaStream_t st) {
+    switch (shader) {
+    case EUC_SHADER_FLAT: launch_vertex<FlatFn>(sc, vb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_VCOLOR: launch_vertex<VColorFn>(sc, vb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_GOURAUD: launch_vertex<GouraudFn>(sc, vb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_TEXTURED: launch_vertex<TexturedFn>(sc, vb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_PHONG: launch_vertex<PhongFn>(sc, vb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_SHADOW: launch_vertex<ShadowFn>(sc, vb, s0, s1, blk0, nblk, ctx, st); break;
+    }
+}
+
+void dispatch_resolve(uint32_t shader, const SceneDev *sc, const uint64_t *pb, int s0, int s1, uint64_t blk0,
+                      uint64_t nblk, euc_ctx *ctx, cudaStream_t st) {
+    switch (shader) {
+    case EUC_SHADER_FLAT: launch_resolve<FlatFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_VCOLOR: launch_resolve<VColorFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_GOURAUD: launch_resolve<GouraudFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_TEXTURED: launch_resolve<TexturedFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_PHONG: launch_resolve<PhongFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_SHADOW: launch_resolve<ShadowFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
+    }
+}
+
+// Runs a batch of scenes.  All pointers inside `scenes` are device pointers.
+int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) {
+    std::vector<Plan> plans;
+    plans.reserve(n);
+    for (size_t i = 0; i < n; ++i) {
+        Plan p;
+        if (int rc = plan_scene(scenes[i], p)) return rc;
+        if (!p.skip) plans.push_back(p);
+    }
+    ctx->last_nscenes = (int)plans.size();
+    if (plans.empty()) return EUC_OK;
+    // group scenes by shader kind so that each kind owns contiguous ranges
+    std::stable_sort(plans.begin(), plans.end(), [](const Plan &a, const Plan &b) { return a.d.shader < b.d.shader; });
+    const int ns = (int)plans.size();
+    uint64_t vtx = 0, vd = 0, tri = 0, pix = 0;
+    for (auto &p : plans) {
+        p.d.vtx_base = vtx;
+        p.d.vd_base = vd;
+        p.d.tri_base = tri;
+        p.d.pix_base = pix;
+        vtx += pad_up(p.d.nverts, kBlock);
+        vd += p.d.nverts * p.nv;
+        tri += pad_up(std::max<uint64_t>(p.d.ngroups, 1), kBlock);
+        pix += pad_up((uint64_t)p.d.W * p.d.H, kBlock);
+    }
+    if (tri >= 0x7FFFFFF0ull) return EUC_ERR_CAPACITY;  // visibility keys hold a 31-bit primitive id
+    const uint64_t nchunks = tri / kBlock;
+    const uint64_t nscan = (tri + kScanBlock - 1) / kScanBlock;
+    int rc;
+    if ((rc = grow(ctx->clip, std::max<uint64_t>(vtx, 1) * sizeof(float4)))) return rc;
+    if ((rc = grow(ctx->vdata, std::max<uint64_t>(vd, 1) * sizeof(float)))) return rc;
+    if ((rc = grow(ctx->recs, tri * sizeof(TriRec)))) return rc;
+    if ((rc = grow(ctx->rows, tri * sizeof(uint32_t)))) return rc;
+    if ((rc = grow(ctx->chunk_sums, nchunks * sizeof(uint2)))) return rc;
+    if ((rc = grow(ctx->live_tri, tri * sizeof(uint32_t)))) return rc;
+    if ((rc = grow(ctx->live_rowoff, tri * sizeof(uint64_t)))) return rc;
+    if ((rc = grow(ctx->totals, 2 * sizeof(unsigned long long)))) return rc;
+    if ((rc = grow(ctx->vbuf, pix * sizeof(unsigned long long)))) return rc;
+    if ((rc = grow(ctx->err, ns * sizeof(int)))) return rc;
+    if ((rc = grow(ctx->stats, ns * sizeof(SceneStats)))) return rc;
+    // staging: scene table | vtx bases | tri bases | pix bases | uniforms
+    const size_t off_sc = 0;
+    const size_t off_vb = pad_up(ns * sizeof(SceneDev), 16);
+    const size_t off_tb = off_vb + pad_up(ns * sizeof(uint64_t), 16);
+    const size_t off_pb = off_tb + pad_up(ns * sizeof(uint64_t), 16);
+    size_t off_u = off_pb + pad_up(ns * sizeof(uint64_t), 16);
+    std::vector<size_t> uoff(ns);
+    for (int i = 0; i < ns; ++i) {
+        uoff[i] = off_u;
+        off_u += pad_up(plans[i].usize, 16);
+    }
+    StageSlot *slot = nullptr;
+    if ((rc = acquire_slot(ctx, off_u, slot))) return rc;
+    uint8_t *h = (uint8_t *)slot->host;
+    uint8_t *dv = (uint8_t *)slot->dev;
+    SceneDev *hsc = (SceneDev *)(h + off_sc);
+    uint64_t *hvb = (uint64_t *)(h + off_vb), *htb = (uint64_t *)(h + off_tb), *hpb = (uint64_t *)(h + off_pb);
+    for (int i = 0; i < ns; ++i) {
+        std::memcpy(h + uoff[i], plans[i].uniforms, plans[i].usize);
+        plans[i].d.uniforms = dv + uoff[i];
+        hsc[i] = plans[i].d;
+        hvb[i] = plans[i].d.vtx_base;
+        htb[i] = plans[i].d.tri_base;
+        hpb[i] = plans[i].d.pix_base;
+    }
+    CUDA_TRY(cudaMemcpyAsync(slot->dev, slot->host, off_u, cudaMemcpyHostToDevice, st));
+    const SceneDev *dsc = (const SceneDev *)(dv + off_sc);
+    const uint64_t *dvb = (const uint64_t *)(dv + off_vb), *dtb = (const uint64_t *)(dv + off_tb),
+                   *dpb = (const uint64_t *)(dv + off_pb);
+    CUDA_TRY(cudaMemsetAsync(ctx->err.p, 0, ns * sizeof(int), st));
+    CUDA_TRY(cudaMemsetAsync(ctx->stats.p, 0, ns * sizeof(SceneStats), st));
+    // vertex stage, one launch per shader kind
+    for (int a = 0; a < ns;) {
+        int b = a;
+        while (b < ns && plans[b].d.shader == plans[a].d.shader) ++b;
+        const uint64_t blk0 = plans[a].d.vtx_base / kBlock;
+        const uint64_t blk1 = (b < ns ? plans[b].d.vtx_base : vtx) / kBlock;
+        dispatch_vertex(plans[a].d.shader, dsc, dvb, a, b, blk0, blk1 - blk0, ctx, st);
+        a = b;
+    }
+    k_setup<<<(unsigned)nchunks, kBlock, 0, st>>>(dsc, dtb, ns, (const float4 *)ctx->clip.p, (TriRec *)ctx->recs.p,
+                                                   (uint32_t *)ctx->rows.p, (uint2 *)ctx->chunk_sums.p, (int *)ctx->err.p,
+                                                   (SceneStats *)ctx->stats.p);
+    k_scan<<<(unsigned)nscan, kBlock, 0, st>>>((const uint32_t *)ctx->rows.p, (const uint2 *)ctx->chunk_sums.p, tri,
+                                               (uint32_t *)ctx->live_tri.p, (uint64_t *)ctx->live_rowoff.p,
+                                               (unsigned long long *)ctx->totals.p);
+    k_init<<<(unsigned)(pix / kBlock), kBlock, 0, st>>>(dsc, dpb, ns, (unsigned long long *)ctx->vbuf.p);
+    k_raster<<<(unsigned)(ctx->nsm * 8), kBlock, 0, st>>>(dsc, (const TriRec *)ctx->recs.p, (const uint32_t *)ctx->live_tri.p,
+                                                           (const uint64_t *)ctx->live_rowoff.p,
+                                                           (const unsigned long long *)ctx->totals.p, (const int *)ctx->err.p,
+                                                           (unsigned long long *)ctx->vbuf.p, (SceneStats *)ctx->stats.p);
+    for (int a = 0; a < ns;) {
+        int b = a;
+        while (b < ns && plans[b].d.shader == plans[a].d.shader) ++b;
+        const uint64_t blk0 = plans[a].d.pix_base / kBlock;
+        const uint64_t blk1 = (b < ns ? plans[b].d.pix_base : pix) / kBlock;
+        dispatch_resolve(plans[a].d.shader, dsc, dpb, a, b, blk0, blk1 - blk0, ctx, st);
+        a = b;
+    }
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaEventRecord(slot->done, st));
+    slot->pending = true;
+    return EUC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int euc_abi_version(void) { return EUC_ABI_VERSION; }
+
+const char *euc_status_string(int status) {
+    switch (status) {
+    case EUC_OK: return "ok";
+    case EUC_ERR_INVALID: return "invalid argument";
+    case EUC_ERR_SIZE_MISMATCH: return "pixel target size is not compatible with depth target size";
+    case EUC_ERR_INDEX_OOB: return "index out of bounds of the vertex slice";
+    case EUC_ERR_OOM: return "out of device memory";
+    case EUC_ERR_CUDA: return "CUDA error";
+    case EUC_ERR_BAND: return "band height is zero (target wider than 20000 << msaa level)";
+    case EUC_ERR_TIMEOUT: return "bounded device wait timed out";
+    case EUC_ERR_BUDGET: return "request exceeds the framebuffer budget";
+    case EUC_ERR_CAPACITY: return "input exceeds a fixed capacity";
+    default: return "unknown status";
+    }
+}
+
+int euc_ctx_create(int device, euc_ctx **out) {
+    if (!out) return EUC_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return EUC_ERR_INVALID;
+    CUDA_TRY(cudaSetDevice(device));
+    euc_ctx *c = new (std::nothrow) euc_ctx();
+    if (!c) return EUC_ERR_OOM;
+    c->device = device;
+    if (cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+        delete c;
+        return EUC_ERR_CUDA;
+    }
+    *out = c;
+    return EUC_OK;
+}
+
+int euc_ctx_destroy(euc_ctx *ctx) {
+    if (!ctx) return EUC_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    DevBuf *bufs[] = {&ctx->clip, &ctx->vdata, &ctx->recs, &ctx->rows, &ctx->chunk_sums, &ctx->live_tri,
+                      &ctx->live_rowoff, &ctx->totals, &ctx->vbuf, &ctx->err, &ctx->stats, &ctx->h_verts,
+                      &ctx->h_idx, &ctx->h_pixel, &ctx->h_depth, &ctx->h_tex[0], &ctx->h_tex[1]};
+    for (DevBuf *b : bufs)
+        if (b->p) cudaFree(b->p);
+    for (auto &s : ctx->slots) {
+        if (s.host) cudaFreeHost(s.host);
+        if (s.dev) cudaFree(s.dev);
+        if (s.done) cudaEventDestroy(s.done);
+    }
+    delete ctx;
+    return EUC_OK;
+}
+
+int euc_ctx_reserve(euc_ctx *ctx, uint64_t max_verts, uint64_t max_tris, uint64_t max_pixels, uint64_t max_scenes) {
+    if (!ctx) return EUC_ERR_INVALID;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CUDA_TRY(cudaSetDevice(ctx->device));
+    const uint64_t ns = std::max<uint64_t>(max_scenes, 1);
+    const uint64_t vtx = max_verts + ns * kBlock, tri = max_tris + ns * kBlock, pix = max_pixels + ns * kBlock;
+    int rc;
+    if ((rc = grow(ctx->clip, vtx * sizeof(float4)))) return rc;
+    if ((rc = grow(ctx->vdata, vtx * 11 * sizeof(float)))) return rc;
+    if ((rc = grow(ctx->recs, tri * sizeof(TriRec)))) return rc;
+    if ((rc = grow(ctx->rows, tri * sizeof(uint32_t)))) return rc;
+    if ((rc = grow(ctx->chunk_sums, (tri / kBlock + 1) * sizeof(uint2)))) return rc;
+    if ((rc = grow(ctx->live_tri, tri * sizeof(uint32_t)))) return rc;
+    if ((rc = grow(ctx->live_rowoff, tri * sizeof(uint64_t)))) return rc;
+    if ((rc = grow(ctx->totals, 2 * sizeof(unsigned long long)))) return rc;
+    if ((rc = grow(ctx->vbuf, pix * sizeof(unsigned long long)))) return rc;
+    if ((rc = grow(ctx->err, ns * sizeof(int)))) return rc;
+    if ((rc = grow(ctx->stats, ns * sizeof(SceneStats)))) return rc;
+    return EUC_OK;
+}
+
+int euc_ctx_sync(euc_ctx *ctx, void *stream) {
+    if (!ctx) return EUC_ERR_INVALID;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CUDA_TRY(cudaSetDevice(ctx->device));
+    CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    if (ctx->last_nscenes == 0 || !ctx->err.p) return EUC_OK;
+    std::vector<int> e(ctx->last_nscenes);
+    CUDA_TRY(cudaMemcpy(e.data(), ctx->err.p, e.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int v : e)
+        if (v) {
+            CUDA_TRY(cudaMemset(ctx->err.p, 0, e.size() * sizeof(int)));
+            return v;
+        }
+    return EUC_OK;
+}
+
+int euc_ctx_stats(euc_ctx *ctx, void *stream, euc_stats *out) {
+    if (!ctx || !out) return EUC_ERR_INVALID;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CUDA_TRY(cudaSetDevice(ctx->device));
+    CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    std::memset(out, 0, sizeof(*out));
+    if (ctx->last_nscenes == 0 || !ctx->stats.p) return EUC_OK;
+    std::vector<SceneStats> s(ctx->last_nscenes);
+    CUDA_TRY(cudaMemcpy(s.data(), ctx->stats.p, s.size() * sizeof(SceneStats), cudaMemcpyDeviceToHost));
+    for (auto &x : s) {
+        out->culled += x.culled;
+        out->candidates += x.candidates;
+    }
+    return EUC_OK;
+}
+
+int euc_render(euc_ctx *ctx, const euc_pipeline_desc *desc, const void *uniforms, size_t uniforms_size,
+               const euc_vertex_layout *layout, const void *vertices, size_t nverts, const uint32_t *indices,
+               size_t nindices, const euc_target *pixel, const euc_target *depth, void *stream) {
+    if (!ctx || !desc || !layout) return EUC_ERR_INVALID;
+    euc_scene s;
+    std::memset(&s, 0, sizeof(s));
+    s.desc = *desc;
+    s.layout = *layout;
+    s.vertices = vertices;
+    s.nverts = nverts;
+    s.indices = indices;
+    s.nindices = nindices;
+    if (pixel) s.pixel = *pixel;
+    if (depth) s.depth = *depth;
+    s.uniforms = uniforms;
+    s.uniforms_size = uniforms_size;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CUDA_TRY(cudaSetDevice(ctx->device));
+    return run_batch(ctx, &s, 1, (cudaStream_t)stream);
+}
+
+int euc_render_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, void *stream) {
+    if (!ctx || (n && !scenes)) return EUC_ERR_INVALID;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CUDA_TRY(cudaSetDevice(ctx->device));
+    return run_batch(ctx, scenes, n, (cudaStream_t)stream);
+}
+
+int euc_render_host(euc_ctx *ctx, const euc_pipeline_desc *desc, const void *uniforms, size_t uniforms_size,
+                    const euc_vertex_layout *layout, const void *vertices, size_t nverts, const uint32_t *indices,
+                    size_t nindices, const euc_target *pixel, const euc_target *depth) {
+    if (!ctx || !desc || !layout || !uniforms) return EUC_ERR_INVALID;
+    const size_t need = uniforms_size_for(desc->shader);
+    if (need == 0 || uniforms_size < need) return EUC_ERR_INVALID;
+    std::unique_lock<std::mutex> g(ctx->mu);
+    CUDA_TRY(cudaSetDevice(ctx->device));
+    int rc;
+    // vertices, indices
+    const size_t vbytes = nverts * layout->stride;
+    if ((rc = grow(ctx->h_verts, std::max<size_t>(vbytes, 4)))) return rc;
+    if (vbytes) CUDA_TRY(cudaMemcpy(ctx->h_verts.p, vertices, vbytes, cudaMemcpyHostToDevice));
+    const uint32_t *didx = nullptr;
+    if (indices) {
+        if ((rc = grow(ctx->h_idx, std::max<size_t>(nindices * 4, 4)))) return rc;
+        if (nindices) CUDA_TRY(cudaMemcpy(ctx->h_idx.p, indices, nindices * 4, cudaMemcpyHostToDevice));
+        didx = (const uint32_t *)ctx->h_idx.p;
+    }
+    // textures: host pointers inside the uniforms become device copies
+    alignas(16) unsigned char ubuf[sizeof(euc_phong_uniforms) + 64];
+    std::memcpy(ubuf, uniforms, need);
+    euc_sampler *samp[2] = {nullptr, nullptr};
+    if (desc->shader == EUC_SHADER_TEXTURED) samp[0] = &((euc_textured_uniforms *)ubuf)->tex;
+    if (desc->shader == EUC_SHADER_PHONG) {
+        samp[0] = &((euc_phong_uniforms *)ubuf)->tex;
+        samp[1] = &((euc_phong_uniforms *)ubuf)->shadow;
+    }
+    for (int k = 0; k < 2; ++k) {
+        if (!samp[k] || !samp[k]->data) continue;
+        if ((rc = check_sampler(*samp[k]))) return rc;
+        const size_t pitch = samp[k]->pitch ? samp[k]->pitch : (size_t)samp[k]->width * 4;
+        const size_t bytes = pitch * samp[k]->height;
+        if ((rc = grow(ctx->h_tex[k], bytes))) return rc;
+        CUDA_TRY(cudaMemcpy(ctx->h_tex[k].p, samp[k]->data, bytes, cudaMemcpyHostToDevice));
+        samp[k]->data = ctx->h_tex[k].p;
+    }
+    // targets
+    euc_target tp = pixel ? *pixel : euc_target{nullptr, 0, 0, 0, EUC_FMT_NONE};
+    euc_target td = depth ? *depth : euc_target{nullptr, 0, 0, 0, EUC_FMT_NONE};
+    void *hp = tp.data, *hd = td.data;
+    size_t pbytes = 0, dbytes = 0;
+    if (hp) {
+        const uint32_t bpp = fmt_bpp(tp.format);
+        if (!bpp) return EUC_ERR_INVALID;
+        const size_t pitch = tp.pitch ? tp.pitch : (size_t)tp.width * bpp;
+        pbytes = pitch * tp.height;
+        if ((rc = grow(ctx->h_pixel, std::max<size_t>(pbytes, 4)))) return rc;
+        CUDA_TRY(cudaMemcpy(ctx->h_pixel.p, hp, pbytes, cudaMemcpyHostToDevice));
+        tp.data = ctx->h_pixel.p;
+    }
+    if (hd) {
+        const size_t pitch = td.pitch ? td.pitch : (size_t)td.width * 4;
+        dbytes = pitch * td.height;
+        if ((rc = grow(ctx->h_depth, std::max<size_t>(dbytes, 4)))) return rc;
+        CUDA_TRY(cudaMemcpy(ctx->h_depth.p, hd, dbytes, cudaMemcpyHostToDevice));
+        td.data = ctx->h_depth.p;
+    }
+    euc_scene s;
+    std::memset(&s, 0, sizeof(s));
+    s.desc = *desc;
+    s.layout = *layout;
+    s.vertices = ctx->h_verts.p;
+    s.nverts = nverts;
+    s.indices = didx;
+    s.nindices = nindices;
+    s.pixel = tp;
+    s.depth = td;
+    s.uniforms = ubuf;
+    s.uniforms_size = need;
+    if ((rc = run_batch(ctx, &s, 1, nullptr))) return rc;
+    CUDA_TRY(cudaStreamSynchronize(nullptr));
+    // device-side errors (index out of bounds) leave the targets untouched
+    if (ctx->last_nscenes) {
+        int e = 0;
+        CUDA_TRY(cudaMemcpy(&e, ctx->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (e) return e;
+    }
+    if (hp) CUDA_TRY(cudaMemcpy(hp, ctx->h_pixel.p, pbytes, cudaMemcpyDeviceToHost));
+    if (hd) CUDA_TRY(cudaMemcpy(hd, ctx->h_depth.p, dbytes, cudaMemcpyDeviceToHost));
+    return EUC_OK;
+}
+
+}  // extern "C"

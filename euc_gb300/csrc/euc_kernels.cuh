@@ -1,0 +1,641 @@
+// euc_kernels.cuh — the GB300 triangle pipeline kernels.
+//
+// Stages (all scenes of a batch go through each stage in one launch):
+//   k_vertex<F>   one thread per unique vertex: the vertex functor
+//                 (pipeline.rs:273-276; shading once per vertex instead of once
+//                 per index gives the same bits because the functor is pure)
+//   k_setup       one thread per primitive: index fetch and bounds check
+//                 (index.rs:52-54), flip, perspective divide, winding, cull /
+//                 reverse, weight matrix, screen bbox, per-pixel weight deltas,
+//                 vertices by y, z-clip class (triangles.rs:55-199)
+//   k_scan        exclusive scan of per-primitive row counts, compaction of the
+//                 primitives that cover at least one row
+//   k_init        per pixel: the visibility key of the depth already in place
+//   k_raster      one thread per (primitive, row): euc's serial f32 weight
+//                 walk along the row span (triangles.rs:219-303), inside test,
+//                 z, z-clip and the depth test against a 64-bit visibility
+//                 key per pixel, merged with atomicMin
+//   k_resolve<F>  per pixel: the winning primitive is shaded once
+//                 (get_v_data, fragment, coarse-grid MSAA, blend) and the
+//                 colour and depth are written (pipeline.rs:529-578)
+//
+// Why an arg-min is exact.  With a blend that ignores the old pixel (every
+// blend in euc's examples), euc's sequential loop leaves in each pixel the
+// fragment of the LAST primitive that passed the depth test.  With a strict
+// test (Less / Greater) and depth writes, that is the first primitive (in
+// submission order) whose z reaches the extreme value, provided it beats the
+// depth already stored; with any other mode the test compares against the
+// unchanged initial depth and the last passing primitive wins.  Both are
+// min-reductions over a 64-bit key, order-independent, so the per-pixel
+// result is bit-identical to euc's loop while rows run in parallel.
+#pragma once
+
+#include "euc_device.cuh"
+
+namespace eucg {
+
+constexpr int kBlock = 256;           // threads per block in every kernel
+constexpr int kScanPer = 8;           // primitives per thread in k_scan
+constexpr int kScanBlock = kBlock * kScanPer;
+
+enum KeyType : uint32_t { KEY_NONE = 0, KEY_MIN = 1, KEY_LAST = 2 };
+
+// One scene of a batch as the kernels see it.
+struct SceneDev {
+    const uint8_t *verts;
+    const uint32_t *idx;      // nullptr: vertices drawn in order
+    const void *uniforms;     // device copy of the shader's uniform struct
+    uint8_t *pixel;
+    uint8_t *depth;
+    uint64_t nverts;
+    uint64_t nstream;         // stream elements (indices, or vertices)
+    uint64_t vtx_base;        // first slot of this scene in clip[]
+    uint64_t vd_base;         // first float of this scene in vdata[]
+    uint64_t tri_base;        // first primitive record (multiple of kBlock)
+    uint64_t pix_base;        // first visibility key (multiple of kBlock)
+    euc_vertex_layout lay;
+    uint32_t ntris;           // complete primitives
+    uint32_t ngroups;         // ceil(nstream / 3): groups whose indices are checked
+    uint32_t W, H, gr, level;
+    uint32_t ppitch, dpitch, pfmt;
+    uint32_t pixel_write, depth_test, depth_write, yflip, zclip, cull, blend, keytype;
+    float zmin, zmax;
+    uint32_t shader, pad0;
+};
+
+// Per-primitive record written by k_setup (128 bytes, 16-byte aligned).
+struct __align__(16) TriRec {
+    float o[3];    // w_hom_origin   (triangles.rs:143)
+    float dx[3];   // w_hom_dx       (triangles.rs:144)
+    float dy[3];   // w_hom_dy       (triangles.rs:145)
+    float zc[3];   // clip-space z of the (reordered) vertices (triangles.rs:269)
+    float vby[6];  // screen vertices ordered by y (triangles.rs:148-171)
+    uint32_t bx0, bx1, by0, by1;  // bbox clamped to the target (band clamp is per row)
+    uint32_t v[3];                // vertex ids after the winding reversal
+    uint32_t scene;
+    uint32_t flags;               // bit 0: all vertices pass the z clip
+    uint32_t pad[5];
+};
+static_assert(sizeof(TriRec) == 128, "TriRec must stay 128 bytes");
+
+struct SceneStats {
+    unsigned long long culled;
+    unsigned long long candidates;
+};
+
+// ---------------------------------------------------------------------------
+// Small helpers
+// ---------------------------------------------------------------------------
+EUC_DEV int find_scene(const uint64_t *base, int n, uint64_t pos) {
+    int lo = 0, hi = n;  // largest i with base[i] <= pos
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (base[mid] <= pos) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Order-preserving map of a non-NaN float onto uint32.
+EUC_DEV uint32_t ord_f32(float f) {
+    uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+EUC_DEV float unord_f32(uint32_t o) {
+    return __uint_as_float((o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o);
+}
+
+// Visibility key of the depth already stored, for KEY_MIN scenes.  A NaN
+// depth fails every comparison, so its key (0) can never be beaten.
+EUC_DEV unsigned long long init_key_min(float d0, bool greater) {
+    if (isnan(d0)) return 0ull;
+    const float c = d0 == 0.0f ? 0.0f : d0;  // -0 and +0 compare equal
+    const uint32_t o = greater ? ~ord_f32(c) : ord_f32(c);
+    return (unsigned long long)o << 32;
+}
+
+template <typename T>
+EUC_DEV T warp_incl_scan(T v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        T n = __shfl_up_sync(0xFFFFFFFFu, v, d);
+        if (lane >= d) v += n;
+    }
+    return v;
+}
+
+template <typename T>
+EUC_DEV T warp_sum(T v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, d);
+    return v;
+}
+
+// Block-wide exclusive scan over kBlock threads; returns the exclusive prefix
+// and writes the block total to *total.
+template <typename T>
+EUC_DEV T block_excl_scan(T v, T *smem /* >= kBlock/32 + 1 */, T *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T inc = warp_incl_scan(v);
+    if (lane == 31) smem[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        T s = lane < kBlock / 32 ? smem[lane] : T(0);
+        T si = warp_incl_scan(s);
+        if (lane < kBlock / 32) smem[lane] = si - s;
+        if (lane == kBlock / 32 - 1) smem[kBlock / 32] = si;
+    }
+    __syncthreads();
+    T r = smem[warp] + inc - v;
+    *total = smem[kBlock / 32];
+    __syncthreads();
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// k_vertex
+// ---------------------------------------------------------------------------
+template <class F>
+__global__ void __launch_bounds__(kBlock) k_vertex(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ vtx_base,
+                                                   int s_begin, int s_end, uint64_t blk_begin, float4 *__restrict__ clip,
+                                                   float *__restrict__ vdata) {
+    __shared__ int s_scene;
+    const uint64_t pos = (blk_begin + blockIdx.x) * (uint64_t)kBlock;
+    if (threadIdx.x == 0) s_scene = s_begin + find_scene(vtx_base + s_begin, s_end - s_begin, pos);
+    __syncthreads();
+    const SceneDev &s = sc[s_scene];
+    const uint64_t v = pos + threadIdx.x - s.vtx_base;
+    if (v >= s.nverts) return;
+    const typename F::U &u = *reinterpret_cast<const typename F::U *>(s.uniforms);
+    float c[4], vd[F::NV];
+    F::vertex(u, s.lay, s.verts + v * s.lay.stride, c, vd);
+    clip[s.vtx_base + v] = make_float4(c[0], c[1], c[2], c[3]);
+    float *out = vdata + s.vd_base + v * F::NV;
+#pragma unroll
+    for (int i = 0; i < F::NV; ++i) out[i] = vd[i];
+}
+
+// ---------------------------------------------------------------------------
+// k_setup: triangles.rs:55-199, once per primitive (euc repeats it per band;
+// only the bbox clamp depends on the band and that is applied per row).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ tri_base,
+                                                  int nsc, const float4 *__restrict__ clip, TriRec *__restrict__ recs,
+                                                  uint32_t *__restrict__ rows, uint2 *__restrict__ chunk_sums,
+                                                  int *__restrict__ err, SceneStats *__restrict__ stats) {
+    __shared__ int s_scene;
+    __shared__ uint32_t s_red[2][kBlock / 32];
+    const uint64_t t = (uint64_t)blockIdx.x * kBlock + threadIdx.x;
+    if (threadIdx.x == 0) s_scene = find_scene(tri_base, nsc, (uint64_t)blockIdx.x * kBlock);
+    __syncthreads();
+    const int si = s_scene;
+    const SceneDev &s = sc[si];
+    const uint64_t lt = t - s.tri_base;
+    uint32_t nrows = 0, culled = 0;
+    if (lt < s.ngroups) {
+        uint32_t vid[3] = {0, 0, 0};
+        bool ok = true;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const uint64_t e = 3 * lt + k;
+            if (e < s.nstream) {
+                const uint64_t id = s.idx ? (uint64_t)__ldg(s.idx + e) : e;
+                if (id >= s.nverts) ok = false;  // index.rs:53 panics on this
+                vid[k] = (uint32_t)id;
+            }
+        }
+        if (!ok) atomicCAS(err + si, 0, EUC_ERR_INDEX_OOB);
+        if (ok && lt < s.ntris) {
+            float h[3][4], e3[3][3];
+            const float flip1 = s.yflip ? -1.0f : 1.0f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float4 c = clip[s.vtx_base + vid[k]];
+                h[k][0] = c.x * 1.0f;
+                h[k][1] = c.y * flip1;
+                h[k][2] = c.z;
+                h[k][3] = c.w;
+                e3[k][0] = h[k][0] / h[k][3];
+                e3[k][1] = h[k][1] / h[k][3];
+                e3[k][2] = h[k][2] / h[k][3];
+            }
+            // winding = cross(e1 - e0, e2 - e0).z   (triangles.rs:67-70)
+            const float ax = e3[1][0] - e3[0][0], ay = e3[1][1] - e3[0][1];
+            const float bx = e3[2][0] - e3[0][0], by = e3[2][1] - e3[0][1];
+            const float winding = ax * by - ay * bx;
+            bool cull = false;
+            if (s.cull != EUC_CULL_NONE) {
+                const float dir = s.cull == EUC_CULL_BACK ? 1.0f : -1.0f;
+                cull = winding * dir < 0.0f;
+            }
+            if (cull) {
+                culled = 1;
+            } else {
+                if (winding >= 0.0f) {  // reverse vertex order (triangles.rs:78-80)
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) { float tmp = h[0][k]; h[0][k] = h[2][k]; h[2][k] = tmp; }
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) { float tmp = e3[0][k]; e3[0][k] = e3[2][k]; e3[2][k] = tmp; }
+                    uint32_t tv = vid[0]; vid[0] = vid[2]; vid[2] = tv;
+                }
+                const float size_x = (float)s.W, size_y = (float)s.H;
+                const float nd[3][3] = {{2.0f / size_x, 0.0f, -1.0f}, {0.0f, -2.0f / size_y, 1.0f}, {0.0f, 0.0f, 1.0f}};
+                // coords_to_weights (triangles.rs:86-102)
+                const float A[3] = {h[0][0], h[0][1], h[0][3]};
+                const float B[3] = {h[1][0], h[1][1], h[1][3]};
+                const float Cc[3] = {h[2][0], h[2][1], h[2][3]};
+                const float ca[3] = {A[0] - Cc[0], A[1] - Cc[1], A[2] - Cc[2]};
+                const float cb[3] = {B[0] - Cc[0], B[1] - Cc[1], B[2] - Cc[2]};
+                const float n[3] = {ca[1] * cb[2] - ca[2] * cb[1], ca[2] * cb[0] - ca[0] * cb[2],
+                                    ca[0] * cb[1] - ca[1] * cb[0]};
+                const float m2 = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+                const float rec_det =
+                    m2 > 0.0f ? 1.0f / rmin(n[0] * Cc[0] + n[1] * Cc[1] + n[2] * Cc[2], -1.1920928955078125e-07f) : 1.0f;
+                float R[3][3] = {{cb[1] * Cc[2] - cb[2] * Cc[1], cb[2] * Cc[0] - cb[0] * Cc[2], cb[0] * Cc[1] - cb[1] * Cc[0]},
+                                 {Cc[1] * ca[2] - Cc[2] * ca[1], Cc[2] * ca[0] - Cc[0] * ca[2], Cc[0] * ca[1] - Cc[1] * ca[0]},
+                                 {n[0], n[1], n[2]}};
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) R[i][j] = R[i][j] * rec_det;
+                float M[3][3];
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) M[i][j] = R[i][0] * nd[0][j] + R[i][1] * nd[1][j] + R[i][2] * nd[2][j];
+                // screen coordinates and bbox (triangles.rs:110-139)
+                float scr[3][2];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    scr[k][0] = size_x * (e3[k][0] * 0.5f + 0.5f);
+                    scr[k][1] = size_y * (e3[k][1] * -0.5f + 0.5f);
+                }
+                const float mnx = rmin(rmin(scr[0][0], scr[1][0]), scr[2][0]);
+                const float mny = rmin(rmin(scr[0][1], scr[1][1]), scr[2][1]);
+                const float mxx = rmax(rmax(scr[0][0], scr[1][0]), scr[2][0]);
+                const float mxy = rmax(rmax(scr[0][1], scr[1][1]), scr[2][1]);
+                const uint32_t bx0 = min(sat_u32(mnx + 0.0f), s.W), bx1 = min(sat_u32(mxx + 1.0f), s.W);
+                const uint32_t by0 = min(sat_u32(mny + 0.0f), s.H), by1 = min(sat_u32(mxy + 1.0f), s.H);
+                // weights at the origin and per pixel (triangles.rs:142-145)
+                float o[3], dxw[3], dyw[3];
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    o[i] = M[i][0] * 0.0f + M[i][1] * 0.0f + M[i][2] * 1.0f;
+                    const float wx = M[i][0] * 1000.0f + M[i][1] * 0.0f + M[i][2] * 1.0f;
+                    const float wy = M[i][0] * 0.0f + M[i][1] * 1000.0f + M[i][2] * 1.0f;
+                    dxw[i] = (wx - o[i]) * (1.0f / 1000.0f);
+                    dyw[i] = (wy - o[i]) * (1.0f / 1000.0f);
+                }
+                // vertices by height (triangles.rs:148-171)
+                const int ord_tab[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+                int oi;
+                if (scr[0][1] == mny) oi = scr[1][1] < scr[2][1] ? 0 : 1;
+                else if (scr[1][1] == mny) oi = scr[0][1] < scr[2][1] ? 2 : 3;
+                else oi = scr[0][1] < scr[1][1] ? 4 : 5;
+                // z-clip class (triangles.rs:173)
+                bool noclip = true;
+                if (s.zclip) {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) noclip = noclip && (s.zmin <= e3[k][2] && e3[k][2] <= s.zmax);
+                }
+                TriRec r;
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    r.o[i] = o[i];
+                    r.dx[i] = dxw[i];
+                    r.dy[i] = dyw[i];
+                    r.zc[i] = h[i][2];
+                }
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    r.vby[2 * k] = scr[ord_tab[oi][k]][0];
+                    r.vby[2 * k + 1] = scr[ord_tab[oi][k]][1];
+                }
+                r.bx0 = bx0; r.bx1 = bx1; r.by0 = by0; r.by1 = by1;
+                r.v[0] = vid[0]; r.v[1] = vid[1]; r.v[2] = vid[2];
+                r.scene = (uint32_t)si;
+                r.flags = noclip ? 1u : 0u;
+#pragma unroll
+                for (int k = 0; k < 5; ++k) r.pad[k] = 0;
+                const float4 *src = reinterpret_cast<const float4 *>(&r);
+                float4 *dst = reinterpret_cast<float4 *>(recs + t);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) dst[k] = src[k];
+                nrows = bx1 > bx0 ? by1 - by0 : 0u;
+            }
+        }
+    }
+    rows[t] = nrows;
+    // per-block sums for the scan, and the culled count of this scene
+    const uint32_t live = nrows ? 1u : 0u;
+    uint32_t wl = warp_sum(live), wr = warp_sum(nrows), wc = warp_sum(culled);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { s_red[0][warp] = wl; s_red[1][warp] = wr; }
+    if (lane == 0 && wc) atomicAdd(&stats[si].culled, (unsigned long long)wc);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t a = 0, b = 0;
+        for (int w = 0; w < kBlock / 32; ++w) { a += s_red[0][w]; b += s_red[1][w]; }
+        chunk_sums[blockIdx.x] = make_uint2(a, b);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_scan: exclusive scan of rows[] and compaction of live primitives.
+// Block b covers primitives [b*kScanBlock, (b+1)*kScanBlock), i.e. the
+// setup chunks [b*kScanPer, (b+1)*kScanPer).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_scan(const uint32_t *__restrict__ rows, const uint2 *__restrict__ chunk_sums,
+                                                 uint64_t ntri, uint32_t *__restrict__ live_tri,
+                                                 uint64_t *__restrict__ live_rowoff, unsigned long long *__restrict__ totals) {
+    __shared__ unsigned long long s_a[kBlock / 32 + 1];
+    __shared__ unsigned long long s_b[kBlock / 32 + 1];
+    __shared__ unsigned long long s_pre[2];
+    // prefix of all earlier chunks
+    const uint64_t nchunk_before = (uint64_t)blockIdx.x * kScanPer;
+    unsigned long long pl = 0, pr = 0;
+    for (uint64_t j = threadIdx.x; j < nchunk_before; j += kBlock) {
+        const uint2 c = chunk_sums[j];
+        pl += c.x;
+        pr += c.y;
+    }
+    unsigned long long tl, tr;
+    block_excl_scan<unsigned long long>(pl, s_a, &tl);
+    block_excl_scan<unsigned long long>(pr, s_b, &tr);
+    if (threadIdx.x == 0) { s_pre[0] = tl; s_pre[1] = tr; }
+    __syncthreads();
+    const unsigned long long base_l = s_pre[0], base_r = s_pre[1];
+    // this thread's kScanPer consecutive primitives
+    const uint64_t t0 = (uint64_t)blockIdx.x * kScanBlock + (uint64_t)threadIdx.x * kScanPer;
+    uint32_t r[kScanPer];
+    unsigned long long my_l = 0, my_r = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {
+        r[k] = t0 + k < ntri ? rows[t0 + k] : 0u;
+        my_l += r[k] ? 1 : 0;
+        my_r += r[k];
+    }
+    unsigned long long bl, br;
+    unsigned long long xl = block_excl_scan<unsigned long long>(my_l, s_a, &bl);
+    unsigned long long xr = block_excl_scan<unsigned long long>(my_r, s_b, &br);
+    unsigned long long ol = base_l + xl, orr = base_r + xr;
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {
+        if (r[k]) {
+            live_tri[ol] = (uint32_t)(t0 + k);
+            live_rowoff[ol] = orr;
+            ++ol;
+            orr += r[k];
+        }
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == kBlock - 1) {
+        totals[0] = base_l + bl;
+        totals[1] = base_r + br;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_init: visibility key of every pixel before rasterisation.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_init(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ pix_base,
+                                                 int nsc, unsigned long long *__restrict__ vbuf) {
+    __shared__ int s_scene;
+    const uint64_t pos = (uint64_t)blockIdx.x * kBlock;
+    if (threadIdx.x == 0) s_scene = find_scene(pix_base, nsc, pos);
+    __syncthreads();
+    const SceneDev &s = sc[s_scene];
+    const uint64_t q = pos + threadIdx.x - s.pix_base;
+    if (q >= (uint64_t)s.W * s.H) return;
+    unsigned long long key = ~0ull;
+    if (s.keytype == KEY_MIN) {
+        const uint32_t x = (uint32_t)(q % s.W), y = (uint32_t)(q / s.W);
+        const float d0 = *reinterpret_cast<const float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x);
+        key = init_key_min(d0, s.depth_test == EUC_TEST_GREATER);
+    }
+    vbuf[s.pix_base + q] = key;
+}
+
+// ---------------------------------------------------------------------------
+// k_raster: one (primitive, row) per thread; persistent over chunks.
+// ---------------------------------------------------------------------------
+EUC_DEV void raster_row(const SceneDev &s, const TriRec &r, uint32_t t, uint32_t y,
+                        unsigned long long *__restrict__ vbuf, uint32_t &cnt) {
+    // band of this row and the band-clamped bbox (pipeline.rs:341-360, triangles.rs:114-139)
+    const uint32_t lo = (y / s.gr) * s.gr;
+    const uint32_t hi = min(lo + s.gr, s.H);
+    const uint32_t by0c = max(r.by0, lo), by1c = min(r.by1, hi);
+    const unsigned long long ext = (unsigned long long)(r.bx1 - r.bx0) * (unsigned long long)(by1c - by0c);
+    const float yf = (float)y;
+    uint32_t xs, xe;
+    if (ext < 128ull) {  // triangles.rs:224-226
+        xs = r.bx0;
+        xe = r.bx1;
+    } else {             // triangles.rs:228-253
+        const float ax = r.vby[0], ay = r.vby[1], bxv = r.vby[2], byv = r.vby[3], cx = r.vby[4], cy = r.vby[5];
+        const float ac = ax + ((yf - ay) / (cy - ay)) * (cx - ax);
+        float lo_f, hi_f;
+        if (yf < byv) {
+            const float ab = ax + ((yf - ay) / (byv - ay)) * (bxv - ax);
+            lo_f = rmin(ab, ac);
+            hi_f = rmax(ab, ac);
+        } else {
+            const float bc = bxv + ((yf - byv) / (cy - byv)) * (cx - bxv);
+            lo_f = rmin(bc, ac);
+            hi_f = rmax(bc, ac);
+        }
+        const float fx0 = (float)r.bx0, fx1 = (float)r.bx1;
+        const float fl = floorf(lo_f), ce = ceilf(hi_f);
+        xs = (fl >= fx0 && fl < fx1) ? sat_u32(fl) : r.bx0;
+        xe = (ce >= fx0 && ce < fx1) ? sat_u32(ce) : r.bx1;
+    }
+    if (xs >= xe) return;
+    // row-start weights, then the serial walk (triangles.rs:257-301)
+    const float xsf = (float)xs;
+    float w0 = (r.o[0] + r.dy[0] * yf) + r.dx[0] * xsf;
+    float w1 = (r.o[1] + r.dy[1] * yf) + r.dx[1] * xsf;
+    float w2 = (r.o[2] + r.dy[2] * yf) + r.dx[2] * xsf;
+    const float d0 = r.dx[0], d1 = r.dx[1], d2 = r.dx[2];
+    const float z0 = r.zc[0], z1 = r.zc[1], z2 = r.zc[2];
+    const bool noclip = r.flags & 1u;
+    unsigned long long *row_keys = vbuf + s.pix_base + (uint64_t)y * s.W;
+    const float *row_depth = s.depth ? reinterpret_cast<const float *>(s.depth + (uint64_t)y * s.dpitch) : nullptr;
+    for (uint32_t x = xs; x < xe; ++x) {
+        const float wu2 = (w2 - w0) - w1;
+        if (w0 >= 0.0f && w1 >= 0.0f && wu2 >= 0.0f) {
+            const float z = (z0 * w0 + z1 * w1) + z2 * wu2;
+            if (noclip || (s.zmin <= z && z <= s.zmax)) {
+                ++cnt;
+                unsigned long long key;
+                bool pass = true;
+                if (s.keytype == KEY_MIN) {
+                    pass = !isnan(z);
+                    const float zc = z == 0.0f ? 0.0f : z;
+                    const uint32_t o = s.depth_test == EUC_TEST_GREATER ? ~ord_f32(zc) : ord_f32(zc);
+                    const uint32_t neg0 = (z == 0.0f && signbit(z)) ? 1u : 0u;
+                    key = ((unsigned long long)o << 32) | (((t + 1u) << 1) | neg0);
+                } else {
+                    if (s.depth_test != EUC_TEST_NONE) {
+                        const float old = row_depth[x];
+                        pass = s.depth_test == EUC_TEST_LESS ? z < old : (s.depth_test == EUC_TEST_EQUAL ? z == old : z > old);
+                    }
+                    key = ((unsigned long long)(~t) << 32) | __float_as_uint(z);
+                }
+                if (pass) {
+                    const unsigned long long cur = __ldcg(row_keys + x);
+                    if (key < cur) atomicMin(row_keys + x, key);
+                }
+            }
+        }
+        w0 = w0 + d0;
+        w1 = w1 + d1;
+        w2 = w2 + d2;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_raster(const SceneDev *__restrict__ sc, const TriRec *__restrict__ recs,
+                                                   const uint32_t *__restrict__ live_tri,
+                                                   const uint64_t *__restrict__ live_rowoff,
+                                                   const unsigned long long *__restrict__ totals,
+                                                   const int *__restrict__ err, unsigned long long *__restrict__ vbuf,
+                                                   SceneStats *__restrict__ stats) {
+    __shared__ uint64_t s_off[kBlock];
+    __shared__ uint64_t s_l0;
+    const uint64_t nlive = totals[0], nitems = totals[1];
+    for (uint64_t c = blockIdx.x; c * kBlock < nitems; c += gridDim.x) {
+        const uint64_t i0 = c * kBlock;
+        if (threadIdx.x == 0) {  // largest l with live_rowoff[l] <= i0
+            uint64_t lo = 0, hi = nlive;
+            while (hi - lo > 1) {
+                const uint64_t mid = (lo + hi) >> 1;
+                if (live_rowoff[mid] <= i0) lo = mid; else hi = mid;
+            }
+            s_l0 = lo;
+        }
+        __syncthreads();
+        const uint64_t l0 = s_l0;
+        s_off[threadIdx.x] = l0 + threadIdx.x < nlive ? live_rowoff[l0 + threadIdx.x] : ~0ull;
+        __syncthreads();
+        const uint64_t i = i0 + threadIdx.x;
+        uint32_t cnt = 0, scene = 0xFFFFFFFFu;
+        if (i < nitems) {
+            int lo = 0, hi = kBlock;  // largest k with s_off[k] <= i
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (s_off[mid] <= i) lo = mid; else hi = mid;
+            }
+            const uint32_t t = live_tri[l0 + lo];
+            const TriRec &r = recs[t];
+            scene = r.scene;
+            if (!err[scene]) raster_row(sc[scene], r, t, r.by0 + (uint32_t)(i - s_off[lo]), vbuf, cnt);
+        }
+        // candidate counts, aggregated per warp when the warp shares a scene
+        const uint32_t s0 = __shfl_sync(0xFFFFFFFFu, scene, 0);
+        if (__all_sync(0xFFFFFFFFu, scene == s0)) {
+            const uint32_t sum = warp_sum(cnt);
+            if ((threadIdx.x & 31) == 0 && sum && s0 != 0xFFFFFFFFu)
+                atomicAdd(&stats[s0].candidates, (unsigned long long)sum);
+        } else if (cnt && scene != 0xFFFFFFFFu) {
+            atomicAdd(&stats[scene].candidates, (unsigned long long)cnt);
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_resolve<F>: shade the winner of every pixel and write colour / depth.
+// ---------------------------------------------------------------------------
+template <class F>
+EUC_DEV void get_v_data(const TriRec &r, const float *__restrict__ vd0, const float *__restrict__ vd1,
+                        const float *__restrict__ vd2, float xf, float yf, float *out) {  // triangles.rs:274-294
+    float w[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) w[c] = (r.o[c] + r.dy[c] * yf) + r.dx[c] * xf;
+    const float wu2 = (w[2] - w[0]) - w[1];
+    const float rr = 1.0f / w[2];
+    const float p0 = w[0] * rr, p1 = w[1] * rr, p2 = wu2 * rr;
+#pragma unroll
+    for (int i = 0; i < F::NV; ++i) out[i] = (vd0[i] * p0 + vd1[i] * p1) + vd2[i] * p2;
+}
+
+template <class F>
+__global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ pix_base,
+                                                    int s_begin, int s_end, uint64_t blk_begin,
+                                                    const TriRec *__restrict__ recs, const float *__restrict__ vdata,
+                                                    const unsigned long long *__restrict__ vbuf) {
+    __shared__ int s_scene;
+    const uint64_t pos = (blk_begin + blockIdx.x) * (uint64_t)kBlock;
+    if (threadIdx.x == 0) s_scene = s_begin + find_scene(pix_base + s_begin, s_end - s_begin, pos);
+    __syncthreads();
+    const SceneDev &s = sc[s_scene];
+    const uint64_t q = pos + threadIdx.x - s.pix_base;
+    if (q >= (uint64_t)s.W * s.H) return;
+    const unsigned long long key = vbuf[s.pix_base + q];
+    uint32_t t;
+    float z;
+    if (s.keytype == KEY_MIN) {
+        const uint32_t low = (uint32_t)key;
+        if (low == 0) return;
+        t = (low >> 1) - 1u;
+        uint32_t o = (uint32_t)(key >> 32);
+        if (s.depth_test == EUC_TEST_GREATER) o = ~o;
+        z = (low & 1u) ? -0.0f : unord_f32(o);
+    } else {
+        if (key == ~0ull) return;
+        t = ~(uint32_t)(key >> 32);
+        z = __uint_as_float((uint32_t)key);
+    }
+    const uint32_t x = (uint32_t)(q % s.W), y = (uint32_t)(q / s.W);
+    if (s.depth_write) *reinterpret_cast<float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x) = z;
+    if (!s.pixel_write) return;
+    const TriRec &r = recs[t];
+    const typename F::U &u = *reinterpret_cast<const typename F::U *>(s.uniforms);
+    const float *vb = vdata + s.vd_base;
+    const float *v0 = vb + (uint64_t)r.v[0] * F::NV;
+    const float *v1 = vb + (uint64_t)r.v[1] * F::NV;
+    const float *v2 = vb + (uint64_t)r.v[2] * F::NV;
+    float frag[F::NF];
+    if (s.level == 0) {
+        float vd[F::NV];
+        get_v_data<F>(r, v0, v1, v2, (float)x, (float)y, vd);
+        F::fragment(u, vd, frag);
+    } else {  // coarse-grid "MSAA" (pipeline.rs:541-573)
+        const uint32_t L = s.level;
+        const uint32_t lo = (y / s.gr) * s.gr;  // band origin
+        const float div = 1.0f / (float)(1u << L);
+        const float fx = rfract((float)x * div);
+        const float fy = rfract((float)(y - lo) * div);
+        const uint32_t px = x >> L, py = (y - lo) >> L;
+        float t00[F::NF], t10[F::NF], t01[F::NF], t11[F::NF];
+        float vd[F::NV];
+        get_v_data<F>(r, v0, v1, v2, (float)((px + 0u) << L), (float)(lo + ((py + 0u) << L)), vd);
+        F::fragment(u, vd, t00);
+        get_v_data<F>(r, v0, v1, v2, (float)((px + 1u) << L), (float)(lo + ((py + 0u) << L)), vd);
+        F::fragment(u, vd, t10);
+        get_v_data<F>(r, v0, v1, v2, (float)((px + 0u) << L), (float)(lo + ((py + 1u) << L)), vd);
+        F::fragment(u, vd, t01);
+        get_v_data<F>(r, v0, v1, v2, (float)((px + 1u) << L), (float)(lo + ((py + 1u) << L)), vd);
+        F::fragment(u, vd, t11);
+#pragma unroll
+        for (int i = 0; i < F::NF; ++i) {
+            const float a = t00[i] * (1.0f - fy) + t01[i] * fy;
+            const float b = t10[i] * (1.0f - fy) + t11[i] * fy;
+            frag[i] = a * (1.0f - fx) + b * fx;
+        }
+    }
+    const float c0 = frag[0], c1 = F::NF > 1 ? frag[F::NF > 1 ? 1 : 0] : 0.0f;
+    const float c2 = F::NF > 2 ? frag[F::NF > 2 ? 2 : 0] : 0.0f, c3 = F::NF > 3 ? frag[F::NF > 3 ? 3 : 0] : 0.0f;
+    const uint32_t r8 = sat_u8(F::pack(c0)), g8 = sat_u8(F::pack(c1)), b8 = sat_u8(F::pack(c2)), a8 = sat_u8(F::pack(c3));
+    uint8_t *p = s.pixel + (uint64_t)y * s.ppitch;
+    if (s.pfmt == EUC_FMT_RGBA8) {
+        reinterpret_cast<uint32_t *>(p)[x] = r8 | (g8 << 8) | (b8 << 16) | (a8 << 24);
+    } else if (s.pfmt == EUC_FMT_BGRA8) {
+        reinterpret_cast<uint32_t *>(p)[x] = b8 | (g8 << 8) | (r8 << 16) | (a8 << 24);
+    } else {
+        p += 3ull * x;
+        p[0] = (uint8_t)r8;
+        p[1] = (uint8_t)g8;
+        p[2] = (uint8_t)b8;
+    }
+}
+
+}  // namespace eucg

@@ -1,0 +1,151 @@
+"""Runs `scenes.FrameSpec`s on the GPU through the C ABI.
+
+Device memory comes from PyTorch (plumbing only); every render goes through
+`euc_render` / `euc_render_batch` in libeuc_gb300.so.
+"""
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import abi, capi
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return C.c_void_p(stream.cuda_stream)
+
+
+def tensor_target(t, fmt):
+    if t is None:
+        return abi.Target(None, 0, 0, 0, abi.FMT_NONE)
+    return abi.Target(t.data_ptr(), t.shape[1], t.shape[0], t.stride(0) * t.element_size(), fmt)
+
+
+def _tex_info(t):
+    fmt = abi.FMT_R32F if t.dtype == torch.float32 else abi.FMT_RGBA8
+    return t.data_ptr(), t.shape[1], t.shape[0], t.stride(0) * t.element_size(), fmt, t
+
+
+class DeviceFrame:
+    """A FrameSpec whose inputs (vertices, indices, textures) and targets are
+    resident in device memory."""
+
+    def __init__(self, frame, device="cuda:0"):
+        self.frame = frame
+        self.device = torch.device(device)
+        cache = {}
+
+        def up(arr, view=None):
+            if arr is None:
+                return None
+            key = id(arr)
+            if key not in cache:
+                a = np.ascontiguousarray(arr if view is None else arr.view(view))
+                cache[key] = torch.from_numpy(a).to(self.device)
+            return cache[key]
+
+        self.passes = []
+        for p in frame.passes:
+            texs = {s.field: up(s.source) for s in p.samplers if not isinstance(s.source, str)}
+            self.passes.append((up(p.vertices), up(p.indices, np.int32), texs))
+        self.targets = {}
+        for t in frame.targets:
+            if t.fmt == abi.FMT_R32F:
+                self.targets[t.name] = torch.empty((t.height, t.width), dtype=torch.float32, device=self.device)
+            else:
+                self.targets[t.name] = torch.empty((t.height, t.width, t.bpp), dtype=torch.uint8, device=self.device)
+        self._clear_px = {t.name: torch.from_numpy(t.host_alloc()[:1, :1].copy()).to(self.device)
+                          for t in frame.targets if t.fmt != abi.FMT_R32F}
+
+    def clear(self):
+        for t in self.frame.targets:
+            if t.fmt == abi.FMT_R32F:
+                self.targets[t.name].fill_(float(np.float32(t.clear)))
+            else:
+                self.targets[t.name].copy_(self._clear_px[t.name].expand_as(self.targets[t.name]))
+
+    def load_targets(self, host):
+        """Copies host numpy targets (name -> array) into the device targets."""
+        for k, v in host.items():
+            self.targets[k].copy_(torch.from_numpy(np.ascontiguousarray(v)))
+
+    def to_host(self):
+        return {k: v.cpu().numpy() for k, v in self.targets.items()}
+
+    def bound_pass(self, k):
+        """(pass spec, uniforms with device texture pointers, keepalive)."""
+        p = self.frame.passes[k]
+        _, _, texs = self.passes[k]
+        by_field = {s.field: s for s in p.samplers}
+
+        def resolve(src):
+            if isinstance(src, str):
+                return _tex_info(self.targets[src])
+            for f, s in by_field.items():
+                if s.source is src:
+                    return _tex_info(texs[f])
+            raise KeyError("texture not uploaded")
+
+        uni, keep = p.bind_uniforms(resolve)
+        return p, uni, keep
+
+    def scene(self, k):
+        """euc_scene for pass k (device pointers) plus keepalive objects."""
+        p, uni, keep = self.bound_pass(k)
+        v, i, _ = self.passes[k]
+        fmt = self.frame.target(p.pixel).fmt if p.pixel else abi.FMT_NONE
+        s = abi.Scene()
+        s.desc = p.desc
+        s.layout = p.layout
+        s.vertices = v.data_ptr()
+        s.nverts = p.nverts
+        s.indices = i.data_ptr() if i is not None else None
+        s.nindices = i.numel() if i is not None else 0
+        s.pixel = tensor_target(self.targets[p.pixel] if p.pixel else None, fmt)
+        s.depth = tensor_target(self.targets[p.depth] if p.depth else None, abi.FMT_R32F)
+        s.uniforms = C.addressof(uni)
+        s.uniforms_size = C.sizeof(uni)
+        return s, (uni, keep)
+
+
+def render_frame(ctx, dframe, stream=None, clear=True):
+    """Clears the targets (if asked) and runs every pass with euc_render."""
+    if clear:
+        dframe.clear()
+    sp = _stream_ptr(stream)
+    for k, p in enumerate(dframe.frame.passes):
+        p, uni, keep = dframe.bound_pass(k)
+        v, i, _ = dframe.passes[k]
+        fmt = dframe.frame.target(p.pixel).fmt if p.pixel else abi.FMT_NONE
+        pt = tensor_target(dframe.targets[p.pixel] if p.pixel else None, fmt)
+        dt = tensor_target(dframe.targets[p.depth] if p.depth else None, abi.FMT_R32F)
+        rc = ctx.render(p.desc, uni, p.layout, v.data_ptr(), p.nverts, i.data_ptr() if i is not None else None,
+                        i.numel() if i is not None else 0, pt, dt, sp)
+        capi.check(rc, "euc_render(%s pass %d)" % (dframe.frame.name, k))
+        del keep
+    return dframe.targets
+
+
+def render_batch(ctx, dframes, stream=None, clear=True):
+    """Renders many frames with euc_render_batch: pass k of every frame goes
+    into the k-th batch call (passes of one frame stay in order)."""
+    if clear:
+        for f in dframes:
+            f.clear()
+    sp = _stream_ptr(stream)
+    npass = max(len(f.frame.passes) for f in dframes)
+    for k in range(npass):
+        scenes, keep = [], []
+        for f in dframes:
+            if k < len(f.frame.passes):
+                s, kp = f.scene(k)
+                scenes.append(s)
+                keep.append(kp)
+        capi.check(ctx.render_batch(scenes, sp), "euc_render_batch(pass %d)" % k)
+        del keep
+
+
+def frame_stats(ctx, stream=None):
+    return ctx.stats(_stream_ptr(stream))

@@ -1,0 +1,174 @@
+"""GPU pipeline vs the CPU oracle on the same seeded inputs.
+
+Bar: depth bit-exact, per-pass candidate-fragment counts exact, colour exact
+for shaders without transcendental functions and within +-1 LSB per 8-bit
+channel for the Phong shader (powf differs by ulps between libm and CUDA).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from euc_gb300 import abi, scenes
+from frameutil import assert_same_inputs, assert_targets_match, run_gpu, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _sphere(seed=3, **kw):
+    return lambda: scenes.sphere_frame(seed=seed, **kw)
+
+
+def _mod(make, **desc):
+    def wrapped():
+        f = make()
+        for p in f.passes:
+            for k, v in desc.items():
+                setattr(p.desc, k, v)
+        return f
+    return wrapped
+
+
+def _soup(seed=1, w=320, h=180, n=4000, hi=3000.0, **desc):
+    return _mod(lambda: scenes.soup_frame(seed=seed, width=w, height=h, ntris=n, area_hi=hi), **desc)
+
+
+def _clear(make, name, value):
+    def wrapped():
+        f = make()
+        f.target(name).clear = value
+        return f
+    return wrapped
+
+
+def _perspective_soup(seed=7, zclip=True):
+    """Soup with w != 1 and z outside the clip range (per-fragment z clip)."""
+    def make():
+        f = scenes.soup_frame(seed=seed, width=257, height=131, ntris=3000, area_hi=4000.0)
+        p = f.passes[0]
+        rng = np.random.default_rng(seed + 100)
+        vb = p.vertices.reshape(p.nverts, 20).copy()
+        pos = vb[:, :16].copy().view(np.float32).reshape(-1, 4)
+        w = rng.uniform(0.5, 2.0, len(pos)).astype(np.float32)
+        pos[:, 0] *= w
+        pos[:, 1] *= w
+        pos[:, 2] = rng.uniform(-0.3, 1.3, len(pos)).astype(np.float32) * w
+        pos[:, 3] = w
+        vb[:, :16] = pos.view(np.uint8).reshape(-1, 16)
+        p.vertices = vb.reshape(-1)
+        if not zclip:
+            p.desc.z_clip = 0
+        return f
+    return make
+
+
+def _knot(aa, seed=2, w=320, h=180, shadow=256):
+    return lambda: scenes.knot_frame(seed=seed, width=w, height=h, shadow_size=shadow, tubular=180, radial=20,
+                                     tex_size=64, aa_level=aa)
+
+
+def _textured(filt, wrap, seed=4, w=200, h=150):
+    def make():
+        rng = np.random.default_rng(seed)
+        pos, nrm, uv, idx = scenes.uv_sphere(20, 10)
+        uv = uv * 3.0 - 1.0  # exercise the wrap modes outside [0, 1]
+        buf, stride, offs = scenes.pack_vertices(pos, uv)
+        model = scenes.translation(0, 0, 2.6) @ scenes.quat_rotation(rng)
+        proj = scenes.perspective_lh_zo(1.0, w / h, 0.1, 50.0)
+        u = abi.TexturedUniforms()
+        u.mvp = scenes.f32mat(proj @ model)
+        tex = rng.integers(0, 256, (13, 17, 4), dtype=np.uint8)
+        p = scenes.PassSpec(scenes.make_desc(abi.SHADER_TEXTURED), scenes.layout(stride, position=offs[0], uv=offs[1]),
+                            buf, len(pos), idx, u, [scenes.SamplerSpec("tex", tex, filt, wrap, 1.0)],
+                            pixel="color", depth="depth")
+        return scenes.FrameSpec("tex", [scenes.TargetSpec("color", w, h, abi.FMT_BGRA8, 0x20406080),
+                                        scenes.TargetSpec("depth", w, h, abi.FMT_R32F, 1.0)], [p])
+    return make
+
+
+def _flat(seed=6):
+    def make():
+        f = scenes.sphere_frame(seed=seed, width=160, height=120, lon=16, lat=8)
+        p = f.passes[0]
+        u = abi.FlatUniforms()
+        u.mvp = p.uniforms.mvp
+        u.color = (C.c_float * 4)(0.25, 0.5, 0.75, 1.0)
+        p.uniforms = u
+        p.desc.shader = abi.SHADER_FLAT
+        return f
+    return make
+
+
+def _unindexed():
+    def make():
+        f = scenes.soup_frame(seed=9, width=150, height=100, ntris=500, area_hi=800.0)
+        p = f.passes[0]
+        nv = p.nverts
+        vb = p.vertices.reshape(nv, 20)[p.indices].reshape(-1)  # un-permute
+        p.vertices = np.ascontiguousarray(vb)
+        p.indices = None
+        return f
+    return make
+
+
+CASES = {
+    "sphere640x480": (_sphere(seed=3), 0),
+    "sphere_small_odd": (_sphere(seed=5, width=97, height=61, lon=24, lat=12), 0),
+    "sphere_cull_none": (_mod(_sphere(seed=8), cull=abi.CULL_NONE), 0),
+    "sphere_cull_front_yup": (_mod(_sphere(seed=8), cull=abi.CULL_FRONT, y_axis=abi.Y_UP), 0),
+    "sphere_bands_seq": (_mod(_sphere(seed=11), band_rows=abi.BANDS_SEQ), 0),
+    "sphere_bands_7": (_mod(_sphere(seed=11), band_rows=7), 0),
+    "sphere_par_small_fallback": (_sphere(seed=12, width=64, height=64, lon=16, lat=8), 0),
+    "sphere_par_empty": (_mod(_sphere(seed=12, width=64, height=64, lon=16, lat=8), flags=abi.FLAG_PAR_EMPTY), 0),
+    "soup_less": (_soup(), 0),
+    "soup_greater": (_clear(_soup(seed=2, depth_test=abi.TEST_GREATER), "depth", 0.0), 0),
+    "soup_equal_write": (_clear(_soup(seed=3, depth_test=abi.TEST_EQUAL), "depth", 0.5), 0),
+    "soup_none_write": (_soup(seed=4, depth_test=abi.TEST_NONE), 0),
+    "soup_less_pass": (_soup(seed=5, depth_write=0), 0),
+    "soup_depth_only": (_soup(seed=6, pixel_write=0), 0),
+    "soup_color_only": (_soup(seed=13, depth_test=abi.TEST_NONE, depth_write=0), 0),
+    "soup_perspective_zclip": (_perspective_soup(7, True), 0),
+    "soup_perspective_noclip": (_perspective_soup(8, False), 0),
+    "soup_large_tris": (_soup(seed=14, w=640, h=360, n=300, hi=150000.0), 0),
+    "knot_aa0": (_knot(0), 1),
+    "knot_aa1": (_knot(1), 1),
+    "knot_aa2": (_knot(2, seed=3), 1),
+    "knot_aa3": (_knot(3, seed=4, w=333, h=211), 1),
+    "tex_linear_tile": (_textured(abi.FILTER_LINEAR, abi.WRAP_TILE), 0),
+    "tex_linear_clamp": (_textured(abi.FILTER_LINEAR, abi.WRAP_CLAMP), 0),
+    "tex_linear_mirror": (_textured(abi.FILTER_LINEAR, abi.WRAP_MIRROR), 0),
+    "tex_linear_none": (_textured(abi.FILTER_LINEAR, abi.WRAP_NONE), 0),
+    "tex_nearest_tile": (_textured(abi.FILTER_NEAREST, abi.WRAP_TILE), 0),
+    "tex_nearest_clamp": (_textured(abi.FILTER_NEAREST, abi.WRAP_CLAMP), 0),
+    "tex_nearest_mirror": (_textured(abi.FILTER_NEAREST, abi.WRAP_MIRROR), 0),
+    "tex_nearest_none": (_textured(abi.FILTER_NEAREST, abi.WRAP_NONE), 0),
+    "flat": (_flat(), 0),
+    "unindexed": (_unindexed(), 0),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_gpu_matches_oracle(name, gpu_ctx):
+    make, tol = CASES[name]
+    assert_same_inputs(make(), make())
+    ref, ref_stats = run_oracle(make())
+    got, got_stats = run_gpu(gpu_ctx, make())
+    assert [s[0] for s in got_stats] == [s[0] for s in ref_stats]
+    assert [s[1] for s in got_stats] == [s[1] for s in ref_stats], "candidate fragment counts"
+    assert [s[2] for s in got_stats] == [s[2] for s in ref_stats], "culled primitive counts"
+    assert_targets_match(make(), ref, got, color_tol=tol)
+
+
+def test_index_out_of_bounds_draws_nothing(gpu_ctx):
+    def make():
+        f = scenes.sphere_frame(seed=1, width=120, height=90, lon=12, lat=6)
+        f.passes[0].indices = f.passes[0].indices.copy()
+        f.passes[0].indices[-1] = f.passes[0].nverts  # one past the end: index.rs:53 panics
+        return f
+    ref, ref_stats = run_oracle(make())
+    got, got_stats = run_gpu(gpu_ctx, make())
+    assert ref_stats[0][0] == abi.ERR_INDEX_OOB
+    assert got_stats[0][0] == abi.ERR_INDEX_OOB
+    clean = make().alloc_host_targets()
+    for k in clean:
+        assert np.array_equal(got[k], clean[k])
