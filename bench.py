@@ -1,0 +1,365 @@
+"""Benchmark of the GB300 euc triangle pipeline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+Workload (one "step" = clear + render of one batch): 256 independent scenes,
+triangle counts log-uniform in [100, 100k] from the sphere / torus-knot / soup
+generators, square resolutions from {64, 128, 256, 512}, half of them with
+Msaa{level: 1}, each with its own 256^2 RGBA8 texture (textured Phong).
+Inputs are synthetic and seeded (no dataset is involved); they stay resident
+in HBM for `value`.
+
+Printed as one JSON line (rank 0):
+  value        batched scenes/s through euc_render_batch (whole job)
+  per_scene    scenes/s for the same scenes through euc_render one at a time
+  e2e          scenes/s through the blocking host-buffer call euc_render_host
+               (host->device copies of inputs and targets, device->host copy of
+               the targets, all inside the timed region)
+  mfrag_per_s  candidate fragments (inside + z-clip, exact counts) per second
+  roofline     algorithmic bytes per batch / the dominant stage's CUDA-event
+               time per batch, against the measured HBM copy bandwidth
+  cpu_baseline the CPU oracle (a port of euc's render_par: row bands over all
+               host threads) on a bounded sample of the same scenes
+
+With --impl reference the CPU oracle is timed alone on the same workload (the
+reference's CPU path; euc itself is Rust and cannot be built here).
+With torchrun (N > 1) every rank renders its own 256 scenes (replicas, no
+collective on the data path) and the slowest rank's time is used.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+N_SCENES = 256
+WORKLOAD = ("256 scenes, tris logU[100,1e5] (sphere/knot/soup), res U{64,128,256,512}^2, "
+            "50% Msaa{level:1}, 256^2 RGBA8 textures, textured Phong")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--scenes", type=int, default=N_SCENES)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-baseline", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_frames(args, rank):
+    from euc_gb300 import scenes
+    return scenes.batch_frames(seed=args.seed + 1000 * rank, n=args.scenes)
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, bus_id=None):
+        self.bus_id = bus_id
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        cmd = ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "200"]
+        if self.bus_id:
+            cmd += ["-i", self.bus_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for l in self.lines:
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (oracle = CPU restatement of euc's render_par)
+# ---------------------------------------------------------------------------
+def cpu_sample(frames, budget_s, start=0):
+    """Renders scenes start, start+1, ... with the oracle on every host thread
+    until `budget_s` has passed; returns (scenes, seconds, threads)."""
+    from oracle import oracle
+    threads = oracle.hw_threads()
+    n, t0 = 0, time.perf_counter()
+    while n < len(frames) and (time.perf_counter() - t0) < budget_s:
+        oracle.run_frame(frames[(start + n) % len(frames)], threads=threads)
+        n += 1
+    return n, time.perf_counter() - t0, threads
+
+
+def run_reference(args):
+    """--impl reference: the CPU oracle alone, on rank 0 only."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    frames = make_frames(args, 0)
+    per_step = max(2.0, 150.0 / max(1, args.steps + args.warmup))
+    pos = 0
+    for _ in range(args.warmup):
+        n, _, _ = cpu_sample(frames, per_step / 4, pos)
+        pos += n
+    total_n, total_t, threads = 0, 0.0, 1
+    for _ in range(args.steps):
+        n, t, threads = cpu_sample(frames, per_step, pos)
+        pos += n
+        total_n += n
+        total_t += t
+    v = total_n / total_t
+    out = {"metric": "scenes/s (batched render, exact coverage)", "impl": "reference", "value": v,
+           "unit": "scenes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * total_t / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators)",
+           "config": {"workload": WORKLOAD, "scenes": args.scenes, "seed": args.seed},
+           "cpu_baseline": {"value": v, "unit": "scenes/s", "cores": threads, "kind": "port",
+                            "sample": "%d scenes (rotating through the 256) in %.1f s" % (total_n, total_t)},
+           "e2e": {"value": v, "unit": "scenes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU legs
+# ---------------------------------------------------------------------------
+def host_bytes(frames):
+    h2d = d2h = 0
+    for f in frames:
+        for p in f.passes:
+            h2d += p.vertices.nbytes + (p.indices.nbytes if p.indices is not None else 0)
+            h2d += sum(s.source.nbytes for s in p.samplers if not isinstance(s.source, str))
+        for t in f.targets:
+            b = t.width * t.height * t.bpp
+            h2d += b
+            d2h += b
+    return h2d, d2h
+
+
+def run_e2e(ctx, frames, reps):
+    """Blocking host-buffer renders (euc_render_host), one per scene pass."""
+    from euc_gb300 import abi
+    hosts = [f.alloc_host_targets() for f in frames]
+    clean = [{k: v.copy() for k, v in h.items()} for h in hosts]
+
+    def one_pass():
+        for f, h, c in zip(frames, hosts, clean):
+            for k in h:
+                np.copyto(h[k], c[k])
+            for p in f.passes:
+                uni, keep = p.bind_uniforms(lambda src: f.host_texture_ptr(src, h))
+                pix = h[p.pixel] if p.pixel else None
+                dep = h[p.depth] if p.depth else None
+                fmt = f.target(p.pixel).fmt if p.pixel else abi.FMT_NONE
+                pt = abi.Target(pix.ctypes.data, pix.shape[1], pix.shape[0], pix.strides[0], fmt) if pix is not None \
+                    else abi.Target(None, 0, 0, 0, 0)
+                dt = abi.Target(dep.ctypes.data, dep.shape[1], dep.shape[0], dep.strides[0], abi.FMT_R32F) \
+                    if dep is not None else abi.Target(None, 0, 0, 0, 0)
+                rc = ctx.render_host(p.desc, uni, p.layout, p.vertices.ctypes.data, p.nverts,
+                                     p.indices.ctypes.data if p.indices is not None else None,
+                                     p.indices.size if p.indices is not None else 0, pt, dt)
+                if rc != abi.OK:
+                    raise RuntimeError("euc_render_host failed: %d" % rc)
+                del keep
+    one_pass()  # warm-up (allocations)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        one_pass()
+    return reps * len(frames) / (time.perf_counter() - t0)
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def load_traffic():
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return None
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+    from euc_gb300 import capi, frames as fr
+
+    world, rank, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = "cuda:%d" % local
+    specs = make_frames(args, rank)
+    ctx = capi.Context(local)
+    batch = fr.DeviceBatch(specs, dev)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        fr.render_batch(ctx, batch, stream, clear=True)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    capi.check(ctx.sync(fr._stream_ptr(stream)), "warm-up")
+    st = ctx.stats(fr._stream_ptr(stream))
+    cand_per_step = st.candidates  # single-pass scenes: one batch call per step
+    ctx.profile()  # reset counters
+
+    bus = None
+    try:
+        bus = torch.cuda.get_device_properties(local).pci_bus_id
+    except AttributeError:
+        pass
+    clocks = ClockSampler(bus)
+    ctx.set_profiling(True)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    ctx.set_profiling(False)
+    stage_ms, launches = ctx.profile()
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * args.scenes / (ms_step / 1e3)
+
+    # per-scene plain path on the same scenes (euc_render, one call per scene)
+    def per_scene_pass():
+        batch.clear()
+        for df in batch.frames:
+            fr.render_frame(ctx, df, stream, clear=False)
+    per_scene_pass()
+    torch.cuda.synchronize()
+    reps = max(2, args.steps // 4)
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for _ in range(reps):
+        per_scene_pass()
+    p1.record(stream)
+    torch.cuda.synchronize()
+    per_scene = args.scenes / (p0.elapsed_time(p1) / reps / 1e3)
+
+    e2e = run_e2e(ctx, specs, reps=1)
+    h2d, d2h = host_bytes(specs)
+
+    alg_bytes = sum(f.algorithmic_bytes() for f in specs)
+    dom = max(stage_ms, key=lambda k: stage_ms[k])
+    dom_ms = stage_ms[dom] / args.steps
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (dom_ms / 1e3) / 1e9
+    traffic = load_traffic()
+    cpu = None
+    if rank == 0 and not args.no_baseline:
+        n, t, threads = cpu_sample(specs, args.cpu_seconds)
+        cpu = {"value": n / t, "unit": "scenes/s", "cores": threads, "kind": "port",
+               "sample": "first %d of the %d scenes in %.1f s (oracle render_par, %d threads)" % (n, len(specs), t, threads)}
+    if rank == 0:
+        out = {
+            "metric": "scenes/s (batched render, exact coverage)", "value": value, "unit": "scenes/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generators), resident in HBM",
+            "config": {"workload": WORKLOAD, "scenes": args.scenes, "seed": args.seed,
+                       "l2": "no flush: %.0f MB of inputs and targets per step > 129 MB L2" % (
+                           (alg_bytes + 8 * sum(t.width * t.height for f in specs for t in f.targets if t.fmt != 4)) / 1e6),
+                       "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "per_scene": {"value": per_scene, "unit": "scenes/s", "path": "euc_render per scene"},
+            "batched_speedup": value / world / per_scene,
+            "mfrag_per_s": cand_per_step * world / (ms_step / 1e3) / 1e6,
+            "mtri_per_s": sum(f.ntris for f in specs) * world / (ms_step / 1e3) / 1e6,
+            "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": "k_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": alg_bytes,
+                         "traffic": traffic.get("k_" + dom) if traffic else None},
+            "e2e": {"value": e2e, "unit": "scenes/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "path": "euc_render_host per scene (host buffers, blocking)"},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(out), flush=True)
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -39,6 +39,9 @@ BANDS_PAR = 0
 BANDS_SEQ = 0xFFFFFFFF
 FLAG_PAR_EMPTY = 1
 
+STAGE_NAMES = ("vertex", "setup", "scan", "init", "raster", "resolve")
+STAGE_COUNT = len(STAGE_NAMES)
+
 FMT_BPP = {FMT_NONE: 0, FMT_RGBA8: 4, FMT_BGRA8: 4, FMT_RGB8: 3, FMT_R32F: 4}
 
 

@@ -27,6 +27,8 @@ SIGNATURES = {
                                   C.POINTER(abi.VertexLayout), C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
                                   C.POINTER(abi.Target), C.POINTER(abi.Target)]),
     "euc_render_batch": (C.c_int, [C.c_void_p, C.POINTER(abi.Scene), C.c_size_t, C.c_void_p]),
+    "euc_ctx_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "euc_ctx_profile": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
 }
 
 
@@ -101,6 +103,16 @@ class Context:
         s = abi.Stats()
         check(lib().euc_ctx_stats(self.handle, stream, C.byref(s)), "euc_ctx_stats")
         return s
+
+    def set_profiling(self, on):
+        check(lib().euc_ctx_set_profiling(self.handle, 1 if on else 0), "euc_ctx_set_profiling")
+
+    def profile(self):
+        """(ms per stage dict, kernel launches) since the last call."""
+        ms = (C.c_double * abi.STAGE_COUNT)()
+        n = C.c_uint64()
+        check(lib().euc_ctx_profile(self.handle, ms, C.byref(n)), "euc_ctx_profile")
+        return dict(zip(abi.STAGE_NAMES, list(ms))), n.value
 
     def render(self, desc, uniforms, layout, vertices_ptr, nverts, indices_ptr, nindices, pixel, depth, stream=None):
         """Raw euc_render: device pointers; returns the status code."""

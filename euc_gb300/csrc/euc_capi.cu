@@ -47,6 +47,12 @@ struct euc_ctx {
     StageSlot slots[kStageSlots];
     int next_slot = 0;
     int last_nscenes = 0;
+    // profiling: event pairs per stage, pooled
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_marks;
+    uint64_t launches = 0;
     std::mutex mu;
 };
 
@@ -271,6 +277,23 @@ int acquire_slot(euc_ctx *ctx, size_t bytes, StageSlot *&out) {
     return EUC_OK;
 }
 
+// Records an event on `st` when profiling; returns nullptr otherwise.
+cudaEvent_t prof_event(euc_ctx *ctx, cudaStream_t st) {
+    if (!ctx->profiling) return nullptr;
+    if (ctx->ev_used == ctx->ev_pool.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        ctx->ev_pool.push_back(e);
+    }
+    cudaEvent_t e = ctx->ev_pool[ctx->ev_used++];
+    cudaEventRecord(e, st);
+    return e;
+}
+
+void prof_mark(euc_ctx *ctx, int stage, cudaEvent_t a, cudaEvent_t b) {
+    if (a && b) ctx->ev_marks.push_back({stage, {a, b}});
+}
+
 template <class F>
 void launch_vertex(const SceneDev *sc, const uint64_t *vb, int s0, int s1, uint64_t blk0, uint64_t nblk, euc_ctx *ctx,
                    cudaStream_t st) {
@@ -381,33 +404,49 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
     CUDA_TRY(cudaMemsetAsync(ctx->err.p, 0, ns * sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(ctx->stats.p, 0, ns * sizeof(SceneStats), st));
     // vertex stage, one launch per shader kind
+    cudaEvent_t e0 = prof_event(ctx, st);
     for (int a = 0; a < ns;) {
         int b = a;
         while (b < ns && plans[b].d.shader == plans[a].d.shader) ++b;
         const uint64_t blk0 = plans[a].d.vtx_base / kBlock;
         const uint64_t blk1 = (b < ns ? plans[b].d.vtx_base : vtx) / kBlock;
         dispatch_vertex(plans[a].d.shader, dsc, dvb, a, b, blk0, blk1 - blk0, ctx, st);
+        ctx->launches += blk1 > blk0;
         a = b;
     }
+    cudaEvent_t e1 = prof_event(ctx, st);
     k_setup<<<(unsigned)nchunks, kBlock, 0, st>>>(dsc, dtb, ns, (const float4 *)ctx->clip.p, (TriRec *)ctx->recs.p,
                                                    (uint32_t *)ctx->rows.p, (uint2 *)ctx->chunk_sums.p, (int *)ctx->err.p,
                                                    (SceneStats *)ctx->stats.p);
+    cudaEvent_t e2 = prof_event(ctx, st);
     k_scan<<<(unsigned)nscan, kBlock, 0, st>>>((const uint32_t *)ctx->rows.p, (const uint2 *)ctx->chunk_sums.p, tri,
                                                (uint32_t *)ctx->live_tri.p, (uint64_t *)ctx->live_rowoff.p,
                                                (unsigned long long *)ctx->totals.p);
+    cudaEvent_t e3 = prof_event(ctx, st);
     k_init<<<(unsigned)(pix / kBlock), kBlock, 0, st>>>(dsc, dpb, ns, (unsigned long long *)ctx->vbuf.p);
+    cudaEvent_t e4 = prof_event(ctx, st);
     k_raster<<<(unsigned)(ctx->nsm * 8), kBlock, 0, st>>>(dsc, (const TriRec *)ctx->recs.p, (const uint32_t *)ctx->live_tri.p,
                                                            (const uint64_t *)ctx->live_rowoff.p,
                                                            (const unsigned long long *)ctx->totals.p, (const int *)ctx->err.p,
                                                            (unsigned long long *)ctx->vbuf.p, (SceneStats *)ctx->stats.p);
+    cudaEvent_t e5 = prof_event(ctx, st);
+    ctx->launches += 4;
     for (int a = 0; a < ns;) {
         int b = a;
         while (b < ns && plans[b].d.shader == plans[a].d.shader) ++b;
         const uint64_t blk0 = plans[a].d.pix_base / kBlock;
         const uint64_t blk1 = (b < ns ? plans[b].d.pix_base : pix) / kBlock;
         dispatch_resolve(plans[a].d.shader, dsc, dpb, a, b, blk0, blk1 - blk0, ctx, st);
+        ctx->launches += blk1 > blk0;
         a = b;
     }
+    cudaEvent_t e6 = prof_event(ctx, st);
+    prof_mark(ctx, EUC_STAGE_VERTEX, e0, e1);
+    prof_mark(ctx, EUC_STAGE_SETUP, e1, e2);
+    prof_mark(ctx, EUC_STAGE_SCAN, e2, e3);
+    prof_mark(ctx, EUC_STAGE_INIT, e3, e4);
+    prof_mark(ctx, EUC_STAGE_RASTER, e4, e5);
+    prof_mark(ctx, EUC_STAGE_RESOLVE, e5, e6);
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaEventRecord(slot->done, st));
     slot->pending = true;
@@ -463,6 +502,7 @@ int euc_ctx_destroy(euc_ctx *ctx) {
                       &ctx->h_idx, &ctx->h_pixel, &ctx->h_depth, &ctx->h_tex[0], &ctx->h_tex[1]};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
+    for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     for (auto &s : ctx->slots) {
         if (s.host) cudaFreeHost(s.host);
         if (s.dev) cudaFree(s.dev);
@@ -490,6 +530,33 @@ int euc_ctx_reserve(euc_ctx *ctx, uint64_t max_verts, uint64_t max_tris, uint64_
     if ((rc = grow(ctx->vbuf, pix * sizeof(unsigned long long)))) return rc;
     if ((rc = grow(ctx->err, ns * sizeof(int)))) return rc;
     if ((rc = grow(ctx->stats, ns * sizeof(SceneStats)))) return rc;
+    return EUC_OK;
+}
+
+int euc_ctx_set_profiling(euc_ctx *ctx, int enable) {
+    if (!ctx) return EUC_ERR_INVALID;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->profiling = enable != 0;
+    return EUC_OK;
+}
+
+int euc_ctx_profile(euc_ctx *ctx, double ms[EUC_STAGE_COUNT], uint64_t *launches) {
+    if (!ctx) return EUC_ERR_INVALID;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CUDA_TRY(cudaSetDevice(ctx->device));
+    double acc[EUC_STAGE_COUNT] = {0, 0, 0, 0, 0, 0};
+    for (auto &m : ctx->ev_marks) {
+        CUDA_TRY(cudaEventSynchronize(m.second.second));
+        float t = 0.0f;
+        CUDA_TRY(cudaEventElapsedTime(&t, m.second.first, m.second.second));
+        acc[m.first] += t;
+    }
+    ctx->ev_marks.clear();
+    ctx->ev_used = 0;
+    if (ms)
+        for (int i = 0; i < EUC_STAGE_COUNT; ++i) ms[i] = acc[i];
+    if (launches) *launches = ctx->launches;
+    ctx->launches = 0;
     return EUC_OK;
 }
 

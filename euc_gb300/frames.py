@@ -110,6 +110,72 @@ class DeviceFrame:
         return s, (uni, keep)
 
 
+class DeviceBatch:
+    """Many DeviceFrames whose colour and depth targets are carved out of two
+    device buffers, so that clearing every target of the batch is two fills
+    (all colour targets of a batch must share one clear value, and so must all
+    depth targets)."""
+
+    def __init__(self, frame_specs, device="cuda:0"):
+        self.frames = []
+        ncol = ndep = 0
+        for f in frame_specs:
+            for t in f.targets:
+                if t.fmt == abi.FMT_R32F:
+                    ndep += t.width * t.height
+                else:
+                    ncol += t.width * t.height * t.bpp + 15
+        dev = torch.device(device)
+        self.color = torch.empty(max(ncol, 1), dtype=torch.uint8, device=dev)
+        self.depth = torch.empty(max(ndep, 1), dtype=torch.float32, device=dev)
+        cclear = {t.clear for f in frame_specs for t in f.targets if t.fmt != abi.FMT_R32F}
+        dclear = {float(np.float32(t.clear)) for f in frame_specs for t in f.targets if t.fmt == abi.FMT_R32F}
+        if len(cclear) > 1 or len(dclear) > 1 or (cclear and next(iter(cclear)) != 0):
+            raise ValueError("DeviceBatch needs one clear value per target kind (colour 0)")
+        self.depth_clear = next(iter(dclear)) if dclear else 1.0
+        co = do = 0
+        for f in frame_specs:
+            df = DeviceFrame.__new__(DeviceFrame)
+            df.frame = f
+            df.device = dev
+            df.targets = {}
+            for t in f.targets:
+                if t.fmt == abi.FMT_R32F:
+                    n = t.width * t.height
+                    df.targets[t.name] = self.depth[do:do + n].view(t.height, t.width)
+                    do += n
+                else:
+                    co = (co + 15) & ~15
+                    n = t.width * t.height * t.bpp
+                    df.targets[t.name] = self.color[co:co + n].view(t.height, t.width, t.bpp)
+                    co += n
+            df._clear_px = {}
+            self.frames.append(df)
+        self._upload(dev)
+
+    def _upload(self, dev):
+        cache = {}
+
+        def up(arr, view=None):
+            if arr is None:
+                return None
+            key = id(arr)
+            if key not in cache:
+                a = np.ascontiguousarray(arr if view is None else arr.view(view))
+                cache[key] = torch.from_numpy(a).to(dev)
+            return cache[key]
+
+        for df in self.frames:
+            df.passes = []
+            for p in df.frame.passes:
+                texs = {s.field: up(s.source) for s in p.samplers if not isinstance(s.source, str)}
+                df.passes.append((up(p.vertices), up(p.indices, np.int32), texs))
+
+    def clear(self):
+        self.color.zero_()
+        self.depth.fill_(self.depth_clear)
+
+
 def render_frame(ctx, dframe, stream=None, clear=True):
     """Clears the targets (if asked) and runs every pass with euc_render."""
     if clear:
@@ -131,7 +197,11 @@ def render_frame(ctx, dframe, stream=None, clear=True):
 def render_batch(ctx, dframes, stream=None, clear=True):
     """Renders many frames with euc_render_batch: pass k of every frame goes
     into the k-th batch call (passes of one frame stay in order)."""
-    if clear:
+    if isinstance(dframes, DeviceBatch):
+        if clear:
+            dframes.clear()
+        dframes = dframes.frames
+    elif clear:
         for f in dframes:
             f.clear()
     sp = _stream_ptr(stream)

@@ -384,6 +384,24 @@ def soup_frame(seed=0, width=1920, height=1080, ntris=200_000, area_lo=1.0, area
                      {"seed": seed, "kind": "soup"})
 
 
+def clip_triangles_frame(clip, colors, width, height, indices=None, pixel_fmt=abi.FMT_RGBA8, depth_clear=1.0,
+                         color_clear=0, **desc):
+    """A one-pass VCOLOR frame from explicit clip-space vertices (n, 4) and
+    RGBA8 colours (n, 4); `desc` overrides make_desc's defaults."""
+    clip = np.asarray(clip, dtype=np.float32).reshape(-1, 4)
+    col = np.asarray(colors, dtype=np.uint8).reshape(-1, 4)
+    vb = np.concatenate([clip.view(np.uint8).reshape(-1, 16), col], axis=1)
+    u = abi.VColorUniforms()
+    u.mvp = f32mat(np.eye(4))
+    kw = dict(cull=abi.CULL_NONE)
+    kw.update(desc)
+    idx = None if indices is None else np.asarray(indices, dtype=np.uint32)
+    p = PassSpec(make_desc(abi.SHADER_VCOLOR, **kw), layout(20, position=0, color=16),
+                 np.ascontiguousarray(vb).reshape(-1), len(clip), idx, u, pixel="color", depth="depth")
+    return FrameSpec("clip_tris", [TargetSpec("color", width, height, pixel_fmt, color_clear),
+                                   TargetSpec("depth", width, height, abi.FMT_R32F, depth_clear)], [p])
+
+
 def _phong_uniforms(model, view, proj, light_vp, light_pos, cam_pos, normal_sign=1.0):
     u = abi.PhongUniforms()
     u.model = f32mat(model)

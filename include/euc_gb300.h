@@ -238,6 +238,24 @@ int euc_ctx_stats(euc_ctx *ctx, void *stream, euc_stats *out);
 const char *euc_status_string(int status);
 int euc_abi_version(void);
 
+/* Pipeline stages, for per-stage timing.                                    */
+enum euc_stage {
+    EUC_STAGE_VERTEX = 0,  /* vertex functor                                   */
+    EUC_STAGE_SETUP = 1,   /* primitive setup                                  */
+    EUC_STAGE_SCAN = 2,    /* row-count scan + compaction                      */
+    EUC_STAGE_INIT = 3,    /* visibility keys of the stored depth              */
+    EUC_STAGE_RASTER = 4,  /* row walk + depth test                            */
+    EUC_STAGE_RESOLVE = 5, /* shading of the winners + colour / depth writes   */
+    EUC_STAGE_COUNT = 6
+};
+
+/* Profiling aid (no counterpart in euc): while enabled, each render records
+ * CUDA events around its stages on its own stream.  euc_ctx_profile waits for
+ * them, returns the summed milliseconds per stage and the number of kernel
+ * launches issued since the last call, and resets both.                     */
+int euc_ctx_set_profiling(euc_ctx *ctx, int enable);
+int euc_ctx_profile(euc_ctx *ctx, double ms[EUC_STAGE_COUNT], uint64_t *launches);
+
 /* ---- rendering --------------------------------------------------------- */
 
 /* `Pipeline::render(vertices, pixel, depth)` (pipeline.rs:248-300) on device
