@@ -60,7 +60,7 @@ def test_library_loads_and_exports_every_declared_symbol():
     lib = C.CDLL(build.LIB)
     missing = [f for f in declared_functions() if not hasattr(lib, f)]
     assert not missing, missing
-    assert set(declared_functions()) <= set(capi.SIGNATURES) | {"euc_render_noalloc"}
+    assert set(declared_functions()) <= set(capi.SIGNATURES)
     assert lib.euc_abi_version() == abi.ABI_VERSION
 
 
