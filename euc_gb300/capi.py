@@ -29,6 +29,9 @@ SIGNATURES = {
     "euc_render_batch": (C.c_int, [C.c_void_p, C.POINTER(abi.Scene), C.c_size_t, C.c_void_p]),
     "euc_ctx_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "euc_ctx_profile": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
+    "euc_render_noalloc": (C.c_int, [C.POINTER(abi.PipelineDesc), C.c_void_p, C.c_size_t, C.POINTER(abi.VertexLayout),
+                                     C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(abi.Target),
+                                     C.POINTER(abi.Target), C.c_void_p, C.c_void_p]),
 }
 
 

@@ -704,3 +704,191 @@ int euc_render_host(euc_ctx *ctx, const euc_pipeline_desc *desc, const void *uni
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// euc_render_noalloc: one render that allocates nothing.
+//
+// Some callers cannot let a library allocate device memory.  An engine or a
+// plugin host may reserve its whole device-memory budget at start-up and give
+// libraries only the buffers they must touch.  A latency-critical render
+// thread cannot afford cudaMalloc or cudaFree, because both synchronise the
+// whole device.  An euc_ctx grows its scratch buffers on demand, so such a
+// caller cannot use euc_render.  This entry point takes the same inputs and
+// outputs but keeps all of its scratch in one fixed array of this file,
+// g_noalloc_scratch (kNaBytes, about 20.8 MiB).  Every GPU that loads this
+// library holds that array until the process exits.
+//
+// Limits: at most kNaMaxVerts vertices, kNaMaxGroups primitives (index
+// triples), kNaMaxPixels target pixels; larger scenes are rejected with
+// EUC_ERR_CAPACITY before anything is enqueued.
+//
+// Every call uses the same array and leaves its contents behind for the next
+// call.  Each call clears on its stream the parts that must start at zero
+// (error flag, counters).  Two calls whose work overlaps on the GPU (calls on
+// different streams, or from different host threads without ordering) race on
+// the array and corrupt each other's results: issue them on one stream.
+//
+// Set-up: the first call on a device looks up the array's device address for
+// that device (cudaGetSymbolAddress, with that device current) and caches it.
+// That first call should come before any stream capture begins.
+// ===========================================================================
+namespace {
+
+constexpr uint64_t kNaMaxVerts = 65536;
+constexpr uint64_t kNaMaxGroups = 65536;
+constexpr uint64_t kNaMaxPixels = 1ull << 20;
+constexpr int kNaMaxNV = 11;  // PhongFn::NV, the largest VertexData
+constexpr size_t kNaStage = 4096;  // scene table, bases, uniforms
+constexpr size_t kNaOffErr = kNaStage;
+constexpr size_t kNaOffStats = kNaOffErr + 256;
+constexpr size_t kNaOffTotals = kNaOffStats + 256;
+constexpr size_t kNaOffClip = kNaOffTotals + 256;
+constexpr size_t kNaOffVdata = kNaOffClip + kNaMaxVerts * sizeof(float4);
+constexpr size_t kNaOffRecs = kNaOffVdata + kNaMaxVerts * kNaMaxNV * sizeof(float);
+constexpr size_t kNaOffRows = kNaOffRecs + kNaMaxGroups * sizeof(TriRec);
+constexpr size_t kNaOffChunks = kNaOffRows + kNaMaxGroups * sizeof(uint32_t);
+constexpr size_t kNaOffLiveTri = kNaOffChunks + (kNaMaxGroups / kBlock) * sizeof(uint2);
+constexpr size_t kNaOffLiveOff = kNaOffLiveTri + kNaMaxGroups * sizeof(uint32_t);
+constexpr size_t kNaOffVbuf = kNaOffLiveOff + kNaMaxGroups * sizeof(uint64_t);
+constexpr size_t kNaBytes = kNaOffVbuf + kNaMaxPixels * sizeof(unsigned long long);
+static_assert(kNaOffClip % 256 == 0 && kNaOffVdata % 256 == 0 && kNaOffRecs % 256 == 0 && kNaOffRows % 256 == 0 &&
+                  kNaOffChunks % 256 == 0 && kNaOffLiveTri % 256 == 0 && kNaOffLiveOff % 256 == 0 &&
+                  kNaOffVbuf % 256 == 0,
+              "scratch regions must stay 256-byte aligned");
+static_assert(kNaMaxVerts % kBlock == 0 && kNaMaxGroups % kBlock == 0 && kNaMaxPixels % kBlock == 0,
+              "limits must be whole blocks");
+
+constexpr int kNaMaxDevices = 64;
+std::mutex g_na_mu;
+unsigned char *g_na_ptr[kNaMaxDevices];
+int g_na_nsm[kNaMaxDevices];
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+namespace {
+
+// Device address of g_noalloc_scratch on the current device (looked up once).
+int na_scratch(int dev, unsigned char **ptr, int *nsm) {
+    std::lock_guard<std::mutex> g(g_na_mu);
+    if (!g_na_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            (void)cudaGetLastError();
+            return EUC_ERR_CUDA;
+        }
+        int n = 0;
+        e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess || n <= 0) {
+            (void)cudaGetLastError();
+            return EUC_ERR_CUDA;
+        }
+        g_na_ptr[dev] = (unsigned char *)p;
+        g_na_nsm[dev] = n;
+    }
+    *ptr = g_na_ptr[dev];
+    *nsm = g_na_nsm[dev];
+    return EUC_OK;
+}
+
+template <class F>
+void na_vertex_resolve(bool vertex, const SceneDev *sc, const uint64_t *base, uint64_t nblk, unsigned char *a,
+                       cudaStream_t st) {
+    if (!nblk) return;
+    if (vertex)
+        k_vertex<F><<<(unsigned)nblk, kBlock, 0, st>>>(sc, base, 0, 1, 0, (float4 *)(a + kNaOffClip),
+                                                       (float *)(a + kNaOffVdata));
+    else
+        k_resolve<F><<<(unsigned)nblk, kBlock, 0, st>>>(sc, base, 0, 1, 0, (const TriRec *)(a + kNaOffRecs),
+                                                        (const float *)(a + kNaOffVdata),
+                                                        (const unsigned long long *)(a + kNaOffVbuf));
+}
+
+void na_dispatch(bool vertex, uint32_t shader, const SceneDev *sc, const uint64_t *base, uint64_t nblk,
+                 unsigned char *a, cudaStream_t st) {
+    switch (shader) {
+    case EUC_SHADER_FLAT: na_vertex_resolve<FlatFn>(vertex, sc, base, nblk, a, st); break;
+    case EUC_SHADER_VCOLOR: na_vertex_resolve<VColorFn>(vertex, sc, base, nblk, a, st); break;
+    case EUC_SHADER_GOURAUD: na_vertex_resolve<GouraudFn>(vertex, sc, base, nblk, a, st); break;
+    case EUC_SHADER_TEXTURED: na_vertex_resolve<TexturedFn>(vertex, sc, base, nblk, a, st); break;
+    case EUC_SHADER_PHONG: na_vertex_resolve<PhongFn>(vertex, sc, base, nblk, a, st); break;
+    case EUC_SHADER_SHADOW: na_vertex_resolve<ShadowFn>(vertex, sc, base, nblk, a, st); break;
+    }
+}
+
+}  // namespace
+
+extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uniforms, size_t uniforms_size,
+                                  const euc_vertex_layout *layout, const void *vertices, size_t nverts,
+                                  const uint32_t *indices, size_t nindices, const euc_target *pixel,
+                                  const euc_target *depth, void *stream, int *device_status) {
+    if (!desc || !layout) return EUC_ERR_INVALID;
+    euc_scene sc;
+    std::memset(&sc, 0, sizeof(sc));
+    sc.desc = *desc;
+    sc.layout = *layout;
+    sc.vertices = vertices;
+    sc.nverts = nverts;
+    sc.indices = indices;
+    sc.nindices = nindices;
+    if (pixel) sc.pixel = *pixel;
+    if (depth) sc.depth = *depth;
+    sc.uniforms = uniforms;
+    sc.uniforms_size = uniforms_size;
+    Plan p;
+    if (int rc = plan_scene(sc, p)) return rc;
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNaMaxDevices) return EUC_ERR_INVALID;
+    unsigned char *a = nullptr;
+    int nsm = 0;
+    if (int rc = na_scratch(dev, &a, &nsm)) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (p.skip) {
+        if (device_status) CUDA_TRY(cudaMemsetAsync(device_status, 0, sizeof(int), st));
+        return EUC_OK;
+    }
+    if (p.d.nverts > kNaMaxVerts || p.d.ngroups > kNaMaxGroups || (uint64_t)p.d.W * p.d.H > kNaMaxPixels ||
+        p.nv > (uint32_t)kNaMaxNV)
+        return EUC_ERR_CAPACITY;
+    const uint64_t vtx = pad_up(p.d.nverts, kBlock);
+    const uint64_t tri = pad_up(std::max<uint64_t>(p.d.ngroups, 1), kBlock);
+    const uint64_t pix = pad_up((uint64_t)p.d.W * p.d.H, kBlock);
+    // scene table | vtx base | tri base | pix base | uniforms, staged on the host stack
+    const size_t off_b = pad_up(sizeof(SceneDev), 16);
+    const size_t off_u = off_b + 3 * 16;
+    alignas(16) unsigned char stage[kNaStage];
+    static_assert((sizeof(SceneDev) + 15) / 16 * 16 + 3 * 16 + sizeof(euc_phong_uniforms) <= kNaStage,
+                  "staging area too small");
+    SceneDev d = p.d;
+    d.vtx_base = d.vd_base = d.tri_base = d.pix_base = 0;
+    d.uniforms = a + off_u;
+    std::memset(stage, 0, off_u);
+    std::memcpy(stage, &d, sizeof(d));
+    std::memcpy(stage + off_u, p.uniforms, p.usize);
+    CUDA_TRY(cudaMemcpyAsync(a, stage, off_u + p.usize, cudaMemcpyHostToDevice, st));
+    const SceneDev *dsc = (const SceneDev *)a;
+    const uint64_t *zero_base = (const uint64_t *)(a + off_b);  // every base is 0 for a single scene
+    CUDA_TRY(cudaMemsetAsync(a + kNaOffErr, 0, sizeof(int), st));
+    CUDA_TRY(cudaMemsetAsync(a + kNaOffStats, 0, sizeof(SceneStats), st));
+    na_dispatch(true, d.shader, dsc, zero_base, vtx / kBlock, a, st);
+    k_setup<<<(unsigned)(tri / kBlock), kBlock, 0, st>>>(dsc, zero_base, 1, (const float4 *)(a + kNaOffClip),
+                                                          (TriRec *)(a + kNaOffRecs), (uint32_t *)(a + kNaOffRows),
+                                                          (uint2 *)(a + kNaOffChunks), (int *)(a + kNaOffErr),
+                                                          (SceneStats *)(a + kNaOffStats));
+    k_scan<<<(unsigned)((tri + kScanBlock - 1) / kScanBlock), kBlock, 0, st>>>(
+        (const uint32_t *)(a + kNaOffRows), (const uint2 *)(a + kNaOffChunks), tri, (uint32_t *)(a + kNaOffLiveTri),
+        (uint64_t *)(a + kNaOffLiveOff), (unsigned long long *)(a + kNaOffTotals));
+    k_init<<<(unsigned)(pix / kBlock), kBlock, 0, st>>>(dsc, zero_base, 1, (unsigned long long *)(a + kNaOffVbuf));
+    k_raster<<<(unsigned)(nsm * 8), kBlock, 0, st>>>(
+        dsc, (const TriRec *)(a + kNaOffRecs), (const uint32_t *)(a + kNaOffLiveTri), (const uint64_t *)(a + kNaOffLiveOff),
+        (const unsigned long long *)(a + kNaOffTotals), (const int *)(a + kNaOffErr),
+        (unsigned long long *)(a + kNaOffVbuf), (SceneStats *)(a + kNaOffStats));
+    na_dispatch(false, d.shader, dsc, zero_base, pix / kBlock, a, st);
+    if (device_status)
+        CUDA_TRY(cudaMemcpyAsync(device_status, a + kNaOffErr, sizeof(int), cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(cudaGetLastError());
+    return EUC_OK;
+}

@@ -283,6 +283,24 @@ int euc_render_host(euc_ctx *ctx, const euc_pipeline_desc *desc, const void *uni
  * rendered alone with euc_render.  No counterpart in euc.                   */
 int euc_render_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, void *stream);
 
+/* euc_render without a context and without any allocation.  No counterpart in
+ * euc: it exists for callers that may not allocate device memory, such as an
+ * engine or plugin host that owns a fixed device-memory budget, or a render
+ * thread that cannot pay for cudaMalloc/cudaFree (both synchronise the whole
+ * device).  Scratch lives in one fixed array inside the library (about 20.8
+ * MiB per device that loads it, held until exit).  Limits: 65,536 vertices,
+ * 65,536 primitives (index triples), 1,048,576 target pixels; larger scenes
+ * return EUC_ERR_CAPACITY.  Runs on the current device, ordered on `stream`.
+ * `device_status` (nullable, device memory) receives EUC_OK or
+ * EUC_ERR_INDEX_OOB once the render has run.  All calls share the scratch
+ * array: calls whose work overlaps on the GPU race, so issue them on one
+ * stream.  The first call on a device looks up the array's device address;
+ * make it before any stream capture starts.                                 */
+int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uniforms, size_t uniforms_size,
+                       const euc_vertex_layout *layout, const void *vertices, size_t nverts,
+                       const uint32_t *indices, size_t nindices, const euc_target *pixel,
+                       const euc_target *depth, void *stream, int *device_status);
+
 #ifdef __cplusplus
 }
 #endif
