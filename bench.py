@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-baseline", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
+    ap.add_argument("--only-batched", action="store_true",
+                    help="run only the batched leg (no per-scene, e2e or CPU legs), e.g. under ncu")
     return ap.parse_args()
 
 
@@ -297,18 +299,19 @@ def run_gpu(args):
         batch.clear()
         for df in batch.frames:
             fr.render_frame(ctx, df, stream, clear=False)
-    per_scene_pass()
-    torch.cuda.synchronize()
-    reps = max(2, args.steps // 4)
-    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    p0.record(stream)
-    for _ in range(reps):
+    per_scene = e2e = None
+    if not args.only_batched:
         per_scene_pass()
-    p1.record(stream)
-    torch.cuda.synchronize()
-    per_scene = args.scenes / (p0.elapsed_time(p1) / reps / 1e3)
-
-    e2e = run_e2e(ctx, specs, reps=1)
+        torch.cuda.synchronize()
+        reps = max(2, args.steps // 4)
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        for _ in range(reps):
+            per_scene_pass()
+        p1.record(stream)
+        torch.cuda.synchronize()
+        per_scene = args.scenes / (p0.elapsed_time(p1) / reps / 1e3)
+        e2e = run_e2e(ctx, specs, reps=1)
     h2d, d2h = host_bytes(specs)
 
     alg_bytes = sum(f.algorithmic_bytes() for f in specs)
@@ -318,7 +321,7 @@ def run_gpu(args):
     achieved = alg_bytes / (dom_ms / 1e3) / 1e9
     traffic = load_traffic()
     cpu = None
-    if rank == 0 and not args.no_baseline:
+    if rank == 0 and not args.no_baseline and not args.only_batched:
         n, t, threads = cpu_sample(specs, args.cpu_seconds)
         cpu = {"value": n / t, "unit": "scenes/s", "cores": threads, "kind": "port",
                "sample": "first %d of the %d scenes in %.1f s (oracle render_par, %d threads)" % (n, len(specs), t, threads)}
@@ -333,7 +336,7 @@ def run_gpu(args):
                            (alg_bytes + 8 * sum(t.width * t.height for f in specs for t in f.targets if t.fmt != 4)) / 1e6),
                        "parallelism": "replicas" if world > 1 else "1 GPU"},
             "per_scene": {"value": per_scene, "unit": "scenes/s", "path": "euc_render per scene"},
-            "batched_speedup": value / world / per_scene,
+            "batched_speedup": value / world / per_scene if per_scene else None,
             "mfrag_per_s": cand_per_step * world / (ms_step / 1e3) / 1e6,
             "mtri_per_s": sum(f.ntris for f in specs) * world / (ms_step / 1e3) / 1e6,
             "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()},

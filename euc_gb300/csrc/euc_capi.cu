@@ -42,6 +42,7 @@ struct euc_ctx {
     int device = 0;
     int nsm = 0;
     DevBuf clip, vdata, recs, rows, chunk_sums, live_tri, live_rowoff, totals, vbuf, err, stats;
+    int raster_blocks = 0;  // resident k_raster blocks per SM
     // buffers used by euc_render_host
     DevBuf h_verts, h_idx, h_pixel, h_depth, h_tex[2];
     StageSlot slots[kStageSlots];
@@ -277,6 +278,20 @@ int acquire_slot(euc_ctx *ctx, size_t bytes, StageSlot *&out) {
     return EUC_OK;
 }
 
+// Resident blocks of k_raster per SM (its grid is persistent).
+int raster_blocks_per_sm() {
+    static int n = 0;
+    if (n == 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_raster, kBlock, 0) != cudaSuccess || b < 1) {
+            (void)cudaGetLastError();
+            b = 4;
+        }
+        n = b;
+    }
+    return n;
+}
+
 // Records an event on `st` when profiling; returns nullptr otherwise.
 cudaEvent_t prof_event(euc_ctx *ctx, cudaStream_t st) {
     if (!ctx->profiling) return nullptr;
@@ -346,16 +361,20 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
     // group scenes by shader kind so that each kind owns contiguous ranges
     std::stable_sort(plans.begin(), plans.end(), [](const Plan &a, const Plan &b) { return a.d.shader < b.d.shader; });
     const int ns = (int)plans.size();
-    uint64_t vtx = 0, vd = 0, tri = 0, pix = 0;
-    for (auto &p : plans) {
+    uint64_t vtx = 0, vd = 0, tri = 0, pix = 0, res = 0;
+    std::vector<uint64_t> res_base(ns);
+    for (int i = 0; i < ns; ++i) {
+        Plan &p = plans[i];
         p.d.vtx_base = vtx;
         p.d.vd_base = vd;
         p.d.tri_base = tri;
         p.d.pix_base = pix;
+        res_base[i] = res;
         vtx += pad_up(p.d.nverts, kBlock);
         vd += p.d.nverts * p.nv;
         tri += pad_up(std::max<uint64_t>(p.d.ngroups, 1), kBlock);
         pix += pad_up((uint64_t)p.d.W * p.d.H, kBlock);
+        res += resolve_blocks(p.d);
     }
     if (tri >= 0x7FFFFFF0ull) return EUC_ERR_CAPACITY;  // visibility keys hold a 31-bit primitive id
     const uint64_t nchunks = tri / kBlock;
@@ -368,7 +387,7 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
     if ((rc = grow(ctx->chunk_sums, nchunks * sizeof(uint2)))) return rc;
     if ((rc = grow(ctx->live_tri, tri * sizeof(uint32_t)))) return rc;
     if ((rc = grow(ctx->live_rowoff, tri * sizeof(uint64_t)))) return rc;
-    if ((rc = grow(ctx->totals, 2 * sizeof(unsigned long long)))) return rc;
+    if ((rc = grow(ctx->totals, 4 * sizeof(unsigned long long)))) return rc;
     if ((rc = grow(ctx->vbuf, pix * sizeof(unsigned long long)))) return rc;
     if ((rc = grow(ctx->err, ns * sizeof(int)))) return rc;
     if ((rc = grow(ctx->stats, ns * sizeof(SceneStats)))) return rc;
@@ -377,7 +396,8 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
     const size_t off_vb = pad_up(ns * sizeof(SceneDev), 16);
     const size_t off_tb = off_vb + pad_up(ns * sizeof(uint64_t), 16);
     const size_t off_pb = off_tb + pad_up(ns * sizeof(uint64_t), 16);
-    size_t off_u = off_pb + pad_up(ns * sizeof(uint64_t), 16);
+    const size_t off_rb = off_pb + pad_up(ns * sizeof(uint64_t), 16);
+    size_t off_u = off_rb + pad_up(ns * sizeof(uint64_t), 16);
     std::vector<size_t> uoff(ns);
     for (int i = 0; i < ns; ++i) {
         uoff[i] = off_u;
@@ -388,7 +408,8 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
     uint8_t *h = (uint8_t *)slot->host;
     uint8_t *dv = (uint8_t *)slot->dev;
     SceneDev *hsc = (SceneDev *)(h + off_sc);
-    uint64_t *hvb = (uint64_t *)(h + off_vb), *htb = (uint64_t *)(h + off_tb), *hpb = (uint64_t *)(h + off_pb);
+    uint64_t *hvb = (uint64_t *)(h + off_vb), *htb = (uint64_t *)(h + off_tb), *hpb = (uint64_t *)(h + off_pb),
+             *hrb = (uint64_t *)(h + off_rb);
     for (int i = 0; i < ns; ++i) {
         std::memcpy(h + uoff[i], plans[i].uniforms, plans[i].usize);
         plans[i].d.uniforms = dv + uoff[i];
@@ -396,11 +417,12 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
         hvb[i] = plans[i].d.vtx_base;
         htb[i] = plans[i].d.tri_base;
         hpb[i] = plans[i].d.pix_base;
+        hrb[i] = res_base[i];
     }
     CUDA_TRY(cudaMemcpyAsync(slot->dev, slot->host, off_u, cudaMemcpyHostToDevice, st));
     const SceneDev *dsc = (const SceneDev *)(dv + off_sc);
     const uint64_t *dvb = (const uint64_t *)(dv + off_vb), *dtb = (const uint64_t *)(dv + off_tb),
-                   *dpb = (const uint64_t *)(dv + off_pb);
+                   *dpb = (const uint64_t *)(dv + off_pb), *drb = (const uint64_t *)(dv + off_rb);
     CUDA_TRY(cudaMemsetAsync(ctx->err.p, 0, ns * sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(ctx->stats.p, 0, ns * sizeof(SceneStats), st));
     // vertex stage, one launch per shader kind
@@ -425,18 +447,18 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
     cudaEvent_t e3 = prof_event(ctx, st);
     k_init<<<(unsigned)(pix / kBlock), kBlock, 0, st>>>(dsc, dpb, ns, (unsigned long long *)ctx->vbuf.p);
     cudaEvent_t e4 = prof_event(ctx, st);
-    k_raster<<<(unsigned)(ctx->nsm * 8), kBlock, 0, st>>>(dsc, (const TriRec *)ctx->recs.p, (const uint32_t *)ctx->live_tri.p,
-                                                           (const uint64_t *)ctx->live_rowoff.p,
-                                                           (const unsigned long long *)ctx->totals.p, (const int *)ctx->err.p,
+    k_raster<<<(unsigned)(ctx->nsm * ctx->raster_blocks), kBlock, 0, st>>>(
+        dsc, (const TriRec *)ctx->recs.p, (const uint32_t *)ctx->live_tri.p, (const uint64_t *)ctx->live_rowoff.p,
+        (unsigned long long *)ctx->totals.p, (const int *)ctx->err.p,
                                                            (unsigned long long *)ctx->vbuf.p, (SceneStats *)ctx->stats.p);
     cudaEvent_t e5 = prof_event(ctx, st);
     ctx->launches += 4;
     for (int a = 0; a < ns;) {
         int b = a;
         while (b < ns && plans[b].d.shader == plans[a].d.shader) ++b;
-        const uint64_t blk0 = plans[a].d.pix_base / kBlock;
-        const uint64_t blk1 = (b < ns ? plans[b].d.pix_base : pix) / kBlock;
-        dispatch_resolve(plans[a].d.shader, dsc, dpb, a, b, blk0, blk1 - blk0, ctx, st);
+        const uint64_t blk0 = res_base[a];
+        const uint64_t blk1 = b < ns ? res_base[b] : res;
+        dispatch_resolve(plans[a].d.shader, dsc, drb, a, b, blk0, blk1 - blk0, ctx, st);
         ctx->launches += blk1 > blk0;
         a = b;
     }
@@ -485,6 +507,7 @@ int euc_ctx_create(int device, euc_ctx **out) {
     euc_ctx *c = new (std::nothrow) euc_ctx();
     if (!c) return EUC_ERR_OOM;
     c->device = device;
+    c->raster_blocks = raster_blocks_per_sm();
     if (cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
         delete c;
         return EUC_ERR_CUDA;
@@ -497,8 +520,8 @@ int euc_ctx_destroy(euc_ctx *ctx) {
     if (!ctx) return EUC_ERR_INVALID;
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
-    DevBuf *bufs[] = {&ctx->clip, &ctx->vdata, &ctx->recs, &ctx->rows, &ctx->chunk_sums, &ctx->live_tri,
-                      &ctx->live_rowoff, &ctx->totals, &ctx->vbuf, &ctx->err, &ctx->stats, &ctx->h_verts,
+    DevBuf *bufs[] = {&ctx->clip, &ctx->vdata, &ctx->recs, &ctx->rows, &ctx->chunk_sums, &ctx->live_tri, &ctx->live_rowoff,
+                      &ctx->totals, &ctx->vbuf, &ctx->err, &ctx->stats, &ctx->h_verts,
                       &ctx->h_idx, &ctx->h_pixel, &ctx->h_depth, &ctx->h_tex[0], &ctx->h_tex[1]};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
@@ -526,7 +549,7 @@ int euc_ctx_reserve(euc_ctx *ctx, uint64_t max_verts, uint64_t max_tris, uint64_
     if ((rc = grow(ctx->chunk_sums, (tri / kBlock + 1) * sizeof(uint2)))) return rc;
     if ((rc = grow(ctx->live_tri, tri * sizeof(uint32_t)))) return rc;
     if ((rc = grow(ctx->live_rowoff, tri * sizeof(uint64_t)))) return rc;
-    if ((rc = grow(ctx->totals, 2 * sizeof(unsigned long long)))) return rc;
+    if ((rc = grow(ctx->totals, 4 * sizeof(unsigned long long)))) return rc;
     if ((rc = grow(ctx->vbuf, pix * sizeof(unsigned long long)))) return rc;
     if ((rc = grow(ctx->err, ns * sizeof(int)))) return rc;
     if ((rc = grow(ctx->stats, ns * sizeof(SceneStats)))) return rc;
@@ -882,11 +905,11 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
         (const uint32_t *)(a + kNaOffRows), (const uint2 *)(a + kNaOffChunks), tri, (uint32_t *)(a + kNaOffLiveTri),
         (uint64_t *)(a + kNaOffLiveOff), (unsigned long long *)(a + kNaOffTotals));
     k_init<<<(unsigned)(pix / kBlock), kBlock, 0, st>>>(dsc, zero_base, 1, (unsigned long long *)(a + kNaOffVbuf));
-    k_raster<<<(unsigned)(nsm * 8), kBlock, 0, st>>>(
+    k_raster<<<(unsigned)(nsm * raster_blocks_per_sm()), kBlock, 0, st>>>(
         dsc, (const TriRec *)(a + kNaOffRecs), (const uint32_t *)(a + kNaOffLiveTri), (const uint64_t *)(a + kNaOffLiveOff),
-        (const unsigned long long *)(a + kNaOffTotals), (const int *)(a + kNaOffErr),
+        (unsigned long long *)(a + kNaOffTotals), (const int *)(a + kNaOffErr),
         (unsigned long long *)(a + kNaOffVbuf), (SceneStats *)(a + kNaOffStats));
-    na_dispatch(false, d.shader, dsc, zero_base, pix / kBlock, a, st);
+    na_dispatch(false, d.shader, dsc, zero_base, resolve_blocks(d), a, st);
     if (device_status)
         CUDA_TRY(cudaMemcpyAsync(device_status, a + kNaOffErr, sizeof(int), cudaMemcpyDeviceToDevice, st));
     CUDA_TRY(cudaGetLastError());

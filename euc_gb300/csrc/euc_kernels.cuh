@@ -341,15 +341,18 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
 }
 
 // ---------------------------------------------------------------------------
-// k_scan: exclusive scan of rows[] and compaction of live primitives.
-// Block b covers primitives [b*kScanBlock, (b+1)*kScanBlock), i.e. the
-// setup chunks [b*kScanPer, (b+1)*kScanPer).
+// k_scan: stable compaction of the primitives that cover at least one row
+// (submission order kept) and the exclusive scan of their row counts.  Block
+// b covers primitives [b*kScanBlock, (b+1)*kScanBlock), i.e. the setup
+// chunks [b*kScanPer, (b+1)*kScanPer).  totals[0] = live primitives,
+// totals[1] = rows, totals[2] = k_raster's work counter (reset here, so that
+// no separate memset is needed).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kBlock) k_scan(const uint32_t *__restrict__ rows, const uint2 *__restrict__ chunk_sums,
                                                  uint64_t ntri, uint32_t *__restrict__ live_tri,
-                                                 uint64_t *__restrict__ live_rowoff, unsigned long long *__restrict__ totals) {
+                                                 uint64_t *__restrict__ live_rowoff,
+                                                 unsigned long long *__restrict__ totals) {
     __shared__ unsigned long long s_a[kBlock / 32 + 1];
-    __shared__ unsigned long long s_b[kBlock / 32 + 1];
     __shared__ unsigned long long s_pre[2];
     // prefix of all earlier chunks
     const uint64_t nchunk_before = (uint64_t)blockIdx.x * kScanPer;
@@ -361,7 +364,7 @@ __global__ void __launch_bounds__(kBlock) k_scan(const uint32_t *__restrict__ ro
     }
     unsigned long long tl, tr;
     block_excl_scan<unsigned long long>(pl, s_a, &tl);
-    block_excl_scan<unsigned long long>(pr, s_b, &tr);
+    block_excl_scan<unsigned long long>(pr, s_a, &tr);
     if (threadIdx.x == 0) { s_pre[0] = tl; s_pre[1] = tr; }
     __syncthreads();
     const unsigned long long base_l = s_pre[0], base_r = s_pre[1];
@@ -376,9 +379,8 @@ __global__ void __launch_bounds__(kBlock) k_scan(const uint32_t *__restrict__ ro
         my_r += r[k];
     }
     unsigned long long bl, br;
-    unsigned long long xl = block_excl_scan<unsigned long long>(my_l, s_a, &bl);
-    unsigned long long xr = block_excl_scan<unsigned long long>(my_r, s_b, &br);
-    unsigned long long ol = base_l + xl, orr = base_r + xr;
+    unsigned long long ol = base_l + block_excl_scan<unsigned long long>(my_l, s_a, &bl);
+    unsigned long long orr = base_r + block_excl_scan<unsigned long long>(my_r, s_a, &br);
 #pragma unroll
     for (int k = 0; k < kScanPer; ++k) {
         if (r[k]) {
@@ -391,6 +393,7 @@ __global__ void __launch_bounds__(kBlock) k_scan(const uint32_t *__restrict__ ro
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == kBlock - 1) {
         totals[0] = base_l + bl;
         totals[1] = base_r + br;
+        totals[2] = 0;
     }
 }
 
@@ -459,85 +462,142 @@ EUC_DEV void raster_row(const SceneDev &s, const TriRec &r, uint32_t t, uint32_t
     const bool noclip = r.flags & 1u;
     unsigned long long *row_keys = vbuf + s.pix_base + (uint64_t)y * s.W;
     const float *row_depth = s.depth ? reinterpret_cast<const float *>(s.depth + (uint64_t)y * s.dpitch) : nullptr;
-    for (uint32_t x = xs; x < xe; ++x) {
-        const float wu2 = (w2 - w0) - w1;
-        if (w0 >= 0.0f && w1 >= 0.0f && wu2 >= 0.0f) {
-            const float z = (z0 * w0 + z1 * w1) + z2 * wu2;
-            if (noclip || (s.zmin <= z && z <= s.zmax)) {
-                ++cnt;
-                unsigned long long key;
-                bool pass = true;
-                if (s.keytype == KEY_MIN) {
-                    pass = !isnan(z);
-                    const float zc = z == 0.0f ? 0.0f : z;
-                    const uint32_t o = s.depth_test == EUC_TEST_GREATER ? ~ord_f32(zc) : ord_f32(zc);
-                    const uint32_t neg0 = (z == 0.0f && signbit(z)) ? 1u : 0u;
-                    key = ((unsigned long long)o << 32) | (((t + 1u) << 1) | neg0);
-                } else {
-                    if (s.depth_test != EUC_TEST_NONE) {
-                        const float old = row_depth[x];
-                        pass = s.depth_test == EUC_TEST_LESS ? z < old : (s.depth_test == EUC_TEST_EQUAL ? z == old : z > old);
+    const bool kmin = s.keytype == KEY_MIN, greater = s.depth_test == EUC_TEST_GREATER;
+    const uint32_t tmin = (t + 1u) << 1;
+    const unsigned long long tlast = (unsigned long long)(~t) << 32;
+    // The walk advances pixel by pixel exactly as euc's loop does; candidates
+    // are gathered kWalk at a time so that their key loads are in flight
+    // together instead of one L2 round trip per pixel.
+    constexpr int kWalk = 4;
+    for (uint32_t x = xs; x < xe; x += kWalk) {
+        float zz[kWalk];
+        bool cand[kWalk];
+#pragma unroll
+        for (int k = 0; k < kWalk; ++k) {
+            cand[k] = false;
+            zz[k] = 0.0f;
+            if (x + k < xe) {
+                const float wu2 = (w2 - w0) - w1;
+                if (w0 >= 0.0f && w1 >= 0.0f && wu2 >= 0.0f) {
+                    const float z = (z0 * w0 + z1 * w1) + z2 * wu2;
+                    if (noclip || (s.zmin <= z && z <= s.zmax)) {
+                        cand[k] = true;
+                        zz[k] = z;
                     }
-                    key = ((unsigned long long)(~t) << 32) | __float_as_uint(z);
                 }
-                if (pass) {
-                    const unsigned long long cur = __ldcg(row_keys + x);
-                    if (key < cur) atomicMin(row_keys + x, key);
-                }
+                w0 = w0 + d0;
+                w1 = w1 + d1;
+                w2 = w2 + d2;
             }
         }
-        w0 = w0 + d0;
-        w1 = w1 + d1;
-        w2 = w2 + d2;
+        unsigned long long key[kWalk];
+        bool pass[kWalk];
+        float old[kWalk];
+        if (!kmin && s.depth_test != EUC_TEST_NONE) {
+#pragma unroll
+            for (int k = 0; k < kWalk; ++k) old[k] = cand[k] ? row_depth[x + k] : 0.0f;
+        }
+#pragma unroll
+        for (int k = 0; k < kWalk; ++k) {
+            cnt += cand[k] ? 1u : 0u;
+            const float z = zz[k];
+            if (kmin) {
+                pass[k] = cand[k] && !isnan(z);
+                const float zc = z == 0.0f ? 0.0f : z;
+                const uint32_t o = greater ? ~ord_f32(zc) : ord_f32(zc);
+                const uint32_t neg0 = (z == 0.0f && signbit(z)) ? 1u : 0u;
+                key[k] = ((unsigned long long)o << 32) | (tmin | neg0);
+            } else {
+                bool p = cand[k];
+                if (s.depth_test == EUC_TEST_LESS) p = p && z < old[k];
+                else if (s.depth_test == EUC_TEST_EQUAL) p = p && z == old[k];
+                else if (s.depth_test == EUC_TEST_GREATER) p = p && z > old[k];
+                pass[k] = p;
+                key[k] = tlast | __float_as_uint(z);
+            }
+        }
+        unsigned long long cur[kWalk];
+#pragma unroll
+        for (int k = 0; k < kWalk; ++k) cur[k] = pass[k] ? __ldcg(row_keys + x + k) : 0ull;
+#pragma unroll
+        for (int k = 0; k < kWalk; ++k)
+            if (pass[k] && key[k] < cur[k]) atomicMin(row_keys + x + k, key[k]);
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_raster(const SceneDev *__restrict__ sc, const TriRec *__restrict__ recs,
+// Warps are scheduled independently: a warp claims the next kWarpItems
+// (primitive, row) items from a global counter, finds the first primitive of
+// its range with a 32-way search of the row offsets, copies the offsets of
+// the (at most kWarpItems) primitives that the range can touch into shared
+// memory and maps each lane's items with a binary search there.  Rows of one
+// large primitive spread over many warps; no block barrier couples a warp to
+// the slowest row of another warp.
+constexpr int kWarpItems = 256;
+
+__global__ void __launch_bounds__(kBlock, 4) k_raster(const SceneDev *__restrict__ sc, const TriRec *__restrict__ recs,
                                                    const uint32_t *__restrict__ live_tri,
                                                    const uint64_t *__restrict__ live_rowoff,
-                                                   const unsigned long long *__restrict__ totals,
+                                                   unsigned long long *__restrict__ totals,
                                                    const int *__restrict__ err, unsigned long long *__restrict__ vbuf,
                                                    SceneStats *__restrict__ stats) {
-    __shared__ uint64_t s_off[kBlock];
-    __shared__ uint64_t s_l0;
+    __shared__ uint64_t s_off[kBlock / 32][kWarpItems];
+    const int lane = threadIdx.x & 31;
+    uint64_t *off = s_off[threadIdx.x >> 5];
     const uint64_t nlive = totals[0], nitems = totals[1];
-    for (uint64_t c = blockIdx.x; c * kBlock < nitems; c += gridDim.x) {
-        const uint64_t i0 = c * kBlock;
-        if (threadIdx.x == 0) {  // largest l with live_rowoff[l] <= i0
-            uint64_t lo = 0, hi = nlive;
-            while (hi - lo > 1) {
-                const uint64_t mid = (lo + hi) >> 1;
-                if (live_rowoff[mid] <= i0) lo = mid; else hi = mid;
-            }
-            s_l0 = lo;
+    // Warps beyond the number of chunks would only find the counter exhausted;
+    // they leave at once instead of queueing on its atomic.
+    const uint64_t gwarp = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5);
+    if (gwarp * kWarpItems >= nitems) return;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(totals + 2, (unsigned long long)kWarpItems);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= nitems) break;
+        // largest l with live_rowoff[l] <= base; invariant off(lo) <= base < off(hi)
+        uint64_t lo = 0, hi = nlive;
+        while (hi - lo > 32) {
+            const uint64_t step = (hi - lo + 31) / 32;
+            const uint64_t probe = lo + lane * step;
+            const bool le = probe < hi && live_rowoff[probe] <= base;
+            const int k = 31 - __clz(__ballot_sync(0xFFFFFFFFu, le));  // lane 0 always qualifies
+            lo = lo + (uint64_t)k * step;
+            hi = min(lo + step, hi);
         }
-        __syncthreads();
-        const uint64_t l0 = s_l0;
-        s_off[threadIdx.x] = l0 + threadIdx.x < nlive ? live_rowoff[l0 + threadIdx.x] : ~0ull;
-        __syncthreads();
-        const uint64_t i = i0 + threadIdx.x;
-        uint32_t cnt = 0, scene = 0xFFFFFFFFu;
-        if (i < nitems) {
-            int lo = 0, hi = kBlock;  // largest k with s_off[k] <= i
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (s_off[mid] <= i) lo = mid; else hi = mid;
+        {
+            const bool le = lo + lane < hi && live_rowoff[lo + lane] <= base;
+            lo += 31 - __clz(__ballot_sync(0xFFFFFFFFu, le));
+        }
+        const uint64_t l0 = lo;
+        for (int j = lane; j < kWarpItems; j += 32) off[j] = l0 + j < nlive ? live_rowoff[l0 + j] : ~0ull;
+        __syncwarp();
+        uint32_t scene0 = 0xFFFFFFFFu, cnt0 = 0;
+        for (int s = 0; s < kWarpItems / 32; ++s) {
+            const uint64_t i = base + (uint64_t)s * 32 + lane;
+            if (i >= nitems) break;
+            int a = 0, b = kWarpItems;  // the last window entry that starts at or before i
+            while (b - a > 1) {
+                const int mid = (a + b) >> 1;
+                if (off[mid] <= i) a = mid; else b = mid;
             }
-            const uint32_t t = live_tri[l0 + lo];
+            const uint32_t t = live_tri[l0 + a];
             const TriRec &r = recs[t];
-            scene = r.scene;
-            if (!err[scene]) raster_row(sc[scene], r, t, r.by0 + (uint32_t)(i - s_off[lo]), vbuf, cnt);
+            const uint32_t scene = r.scene;
+            if (err[scene]) continue;
+            uint32_t cnt = 0;
+            raster_row(sc[scene], r, t, r.by0 + (uint32_t)(i - off[a]), vbuf, cnt);
+            if (scene0 == 0xFFFFFFFFu) scene0 = scene;
+            if (scene == scene0) cnt0 += cnt;
+            else if (cnt) atomicAdd(&stats[scene].candidates, (unsigned long long)cnt);
         }
-        // candidate counts, aggregated per warp when the warp shares a scene
-        const uint32_t s0 = __shfl_sync(0xFFFFFFFFu, scene, 0);
-        if (__all_sync(0xFFFFFFFFu, scene == s0)) {
-            const uint32_t sum = warp_sum(cnt);
-            if ((threadIdx.x & 31) == 0 && sum && s0 != 0xFFFFFFFFu)
-                atomicAdd(&stats[s0].candidates, (unsigned long long)sum);
-        } else if (cnt && scene != 0xFFFFFFFFu) {
-            atomicAdd(&stats[scene].candidates, (unsigned long long)cnt);
+        // per-lane counts for each lane's first scene; most warps hold one scene
+        const uint32_t s0 = __shfl_sync(0xFFFFFFFFu, scene0, 0);
+        if (__all_sync(0xFFFFFFFFu, scene0 == s0 || cnt0 == 0)) {
+            const uint32_t sum = warp_sum(cnt0);
+            if (lane == 0 && sum) atomicAdd(&stats[s0].candidates, (unsigned long long)sum);
+        } else if (cnt0) {
+            atomicAdd(&stats[scene0].candidates, (unsigned long long)cnt0);
         }
-        __syncthreads();
+        __syncwarp();
     }
 }
 
@@ -557,71 +617,25 @@ EUC_DEV void get_v_data(const TriRec &r, const float *__restrict__ vd0, const fl
     for (int i = 0; i < F::NV; ++i) out[i] = (vd0[i] * p0 + vd1[i] * p1) + vd2[i] * p2;
 }
 
-template <class F>
-__global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ pix_base,
-                                                    int s_begin, int s_end, uint64_t blk_begin,
-                                                    const TriRec *__restrict__ recs, const float *__restrict__ vdata,
-                                                    const unsigned long long *__restrict__ vbuf) {
-    __shared__ int s_scene;
-    const uint64_t pos = (blk_begin + blockIdx.x) * (uint64_t)kBlock;
-    if (threadIdx.x == 0) s_scene = s_begin + find_scene(pix_base + s_begin, s_end - s_begin, pos);
-    __syncthreads();
-    const SceneDev &s = sc[s_scene];
-    const uint64_t q = pos + threadIdx.x - s.pix_base;
-    if (q >= (uint64_t)s.W * s.H) return;
-    const unsigned long long key = vbuf[s.pix_base + q];
-    uint32_t t;
-    float z;
+// Decodes a visibility key; false when no fragment passed at this pixel.
+EUC_DEV bool decode_key(const SceneDev &s, unsigned long long key, uint32_t &t, float &z) {
     if (s.keytype == KEY_MIN) {
         const uint32_t low = (uint32_t)key;
-        if (low == 0) return;
+        if (low == 0) return false;
         t = (low >> 1) - 1u;
         uint32_t o = (uint32_t)(key >> 32);
         if (s.depth_test == EUC_TEST_GREATER) o = ~o;
         z = (low & 1u) ? -0.0f : unord_f32(o);
-    } else {
-        if (key == ~0ull) return;
-        t = ~(uint32_t)(key >> 32);
-        z = __uint_as_float((uint32_t)key);
+        return true;
     }
-    const uint32_t x = (uint32_t)(q % s.W), y = (uint32_t)(q / s.W);
-    if (s.depth_write) *reinterpret_cast<float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x) = z;
-    if (!s.pixel_write) return;
-    const TriRec &r = recs[t];
-    const typename F::U &u = *reinterpret_cast<const typename F::U *>(s.uniforms);
-    const float *vb = vdata + s.vd_base;
-    const float *v0 = vb + (uint64_t)r.v[0] * F::NV;
-    const float *v1 = vb + (uint64_t)r.v[1] * F::NV;
-    const float *v2 = vb + (uint64_t)r.v[2] * F::NV;
-    float frag[F::NF];
-    if (s.level == 0) {
-        float vd[F::NV];
-        get_v_data<F>(r, v0, v1, v2, (float)x, (float)y, vd);
-        F::fragment(u, vd, frag);
-    } else {  // coarse-grid "MSAA" (pipeline.rs:541-573)
-        const uint32_t L = s.level;
-        const uint32_t lo = (y / s.gr) * s.gr;  // band origin
-        const float div = 1.0f / (float)(1u << L);
-        const float fx = rfract((float)x * div);
-        const float fy = rfract((float)(y - lo) * div);
-        const uint32_t px = x >> L, py = (y - lo) >> L;
-        float t00[F::NF], t10[F::NF], t01[F::NF], t11[F::NF];
-        float vd[F::NV];
-        get_v_data<F>(r, v0, v1, v2, (float)((px + 0u) << L), (float)(lo + ((py + 0u) << L)), vd);
-        F::fragment(u, vd, t00);
-        get_v_data<F>(r, v0, v1, v2, (float)((px + 1u) << L), (float)(lo + ((py + 0u) << L)), vd);
-        F::fragment(u, vd, t10);
-        get_v_data<F>(r, v0, v1, v2, (float)((px + 0u) << L), (float)(lo + ((py + 1u) << L)), vd);
-        F::fragment(u, vd, t01);
-        get_v_data<F>(r, v0, v1, v2, (float)((px + 1u) << L), (float)(lo + ((py + 1u) << L)), vd);
-        F::fragment(u, vd, t11);
-#pragma unroll
-        for (int i = 0; i < F::NF; ++i) {
-            const float a = t00[i] * (1.0f - fy) + t01[i] * fy;
-            const float b = t10[i] * (1.0f - fy) + t11[i] * fy;
-            frag[i] = a * (1.0f - fx) + b * fx;
-        }
-    }
+    if (key == ~0ull) return false;
+    t = ~(uint32_t)(key >> 32);
+    z = __uint_as_float((uint32_t)key);
+    return true;
+}
+
+template <class F>
+EUC_DEV void store_pixel(const SceneDev &s, uint32_t x, uint32_t y, const float *frag) {
     const float c0 = frag[0], c1 = F::NF > 1 ? frag[F::NF > 1 ? 1 : 0] : 0.0f;
     const float c2 = F::NF > 2 ? frag[F::NF > 2 ? 2 : 0] : 0.0f, c3 = F::NF > 3 ? frag[F::NF > 3 ? 3 : 0] : 0.0f;
     const uint32_t r8 = sat_u8(F::pack(c0)), g8 = sat_u8(F::pack(c1)), b8 = sat_u8(F::pack(c2)), a8 = sat_u8(F::pack(c3));
@@ -636,6 +650,153 @@ __global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__
         p[1] = (uint8_t)g8;
         p[2] = (uint8_t)b8;
     }
+}
+
+// Row pairs of the level-1 coarse grid: the grid restarts at every band, so a
+// band of odd height ends with a single row.
+__host__ __device__ inline uint64_t quad_row_pairs(uint32_t H, uint32_t gr) {
+    const uint64_t nb = (H + gr - 1) / gr, ppb = (gr + 1) / 2, lh = H - (nb - 1) * gr;
+    return (nb - 1) * ppb + (lh + 1) / 2;
+}
+
+__host__ __device__ inline bool resolve_by_quads(const SceneDev &s) { return s.level == 1 && s.pixel_write; }
+
+// Blocks of k_resolve for one scene.
+__host__ __device__ inline uint64_t resolve_blocks(const SceneDev &s) {
+    if (resolve_by_quads(s)) {
+        const uint64_t warps = quad_row_pairs(s.H, s.gr) * ((s.W + 15) / 16);
+        return (warps + kBlock / 32 - 1) / (kBlock / 32);
+    }
+    return ((uint64_t)s.W * s.H + kBlock - 1) / kBlock;
+}
+
+template <class F>
+__global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ res_base,
+                                                    int s_begin, int s_end, uint64_t blk_begin,
+                                                    const TriRec *__restrict__ recs, const float *__restrict__ vdata,
+                                                    const unsigned long long *__restrict__ vbuf) {
+    __shared__ int s_scene;
+    const uint64_t blk = blk_begin + blockIdx.x;
+    if (threadIdx.x == 0) s_scene = s_begin + find_scene(res_base + s_begin, s_end - s_begin, blk);
+    __syncthreads();
+    const SceneDev &s = sc[s_scene];
+    const uint64_t lb = blk - res_base[s_scene];
+    const int tid = threadIdx.x, lane = tid & 31;
+    // 1. this thread's pixel
+    uint32_t x = 0, y = 0, lo = 0;
+    bool inside;
+    const bool quads = resolve_by_quads(s);
+    if (quads) {  // warp = 16x2 pixels on whole 2x2 cells of the band-relative grid
+        const uint32_t cols = (s.W + 15) >> 4, ppb = (s.gr + 1) >> 1;
+        const uint64_t w = lb * (kBlock / 32) + (tid >> 5);
+        inside = w < quad_row_pairs(s.H, s.gr) * cols;
+        if (inside) {
+            const uint32_t p = (uint32_t)(w / cols), a = (uint32_t)(w % cols);
+            const uint32_t b = p / ppb, k = p % ppb;
+            lo = b * s.gr;
+            x = a * 16 + (lane & 15);
+            y = lo + 2 * k + (lane >> 4);
+            inside = x < s.W && y < min(lo + s.gr, s.H);
+        }
+    } else {
+        const uint64_t q = lb * kBlock + tid;
+        inside = q < (uint64_t)s.W * s.H;
+        if (inside) {
+            x = (uint32_t)(q % s.W);
+            y = (uint32_t)(q / s.W);
+            lo = (y / s.gr) * s.gr;
+        }
+    }
+    uint32_t t = 0xFFFFFFFFu;
+    float z = 0.0f;
+    const bool win = inside && decode_key(s, vbuf[s.pix_base + (uint64_t)y * s.W + x], t, z);
+    if (win && s.depth_write) *reinterpret_cast<float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x) = z;
+    if (!s.pixel_write) return;  // uniform over the block (one scene)
+
+    // 2. the fragment evaluations this block needs, compacted into a job list.
+    // A job is (pixel slot, corner); corner 0 is the pixel itself when there
+    // is no MSAA.  With level-1 MSAA each pixel shades the corner of its 2x2
+    // cell at its own offset and reuses the other three from the cell's other
+    // pixels when they have the same winner.  A coarse fragment is a pure
+    // function of (primitive, grid point), so sharing changes no bits (euc's
+    // own coarse cache, pipeline.rs:477-494, is transparent the same way).
+    __shared__ uint32_t s_t[kBlock];
+    __shared__ uint32_t s_xy[kBlock][3];
+    __shared__ uint16_t s_job[4 * kBlock];
+    __shared__ float s_frag[kBlock][4][F::NF];
+    __shared__ uint32_t s_scan[kBlock / 32 + 1];
+    s_t[tid] = win ? t : 0xFFFFFFFFu;
+    s_xy[tid][0] = x;
+    s_xy[tid][1] = y;
+    s_xy[tid][2] = lo;
+    __syncthreads();
+    const int own_c = (lane & 1) | ((lane >> 4) << 1);
+    uint32_t need = 0;  // bit c: this pixel evaluates corner c itself
+    if (win) {
+        if (s.level == 0) {
+            need = 1u;
+        } else if (quads) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int owner = (tid & ~31) | (lane & ~17) | (c & 1) | ((c >> 1) << 4);
+                if (c == own_c || s_t[owner] != t) need |= 1u << c;
+            }
+        } else {
+            need = 0xFu;
+        }
+    }
+    uint32_t njobs;
+    uint32_t off = block_excl_scan<uint32_t>(__popc(need), s_scan, &njobs);
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+        if (need & (1u << c)) s_job[off++] = (uint16_t)((tid << 2) | c);
+    __syncthreads();
+
+    // 3. every thread evaluates jobs until the list is done
+    const typename F::U &u = *reinterpret_cast<const typename F::U *>(s.uniforms);
+    const float *vb = vdata + s.vd_base;
+    const uint32_t L = s.level;
+    for (uint32_t j = tid; j < njobs; j += kBlock) {
+        const int slot = s_job[j] >> 2, c = s_job[j] & 3;
+        const TriRec &r = recs[s_t[slot]];
+        float xf, yf;
+        if (L == 0) {
+            xf = (float)s_xy[slot][0];
+            yf = (float)s_xy[slot][1];
+        } else {
+            const uint32_t sx = s_xy[slot][0], sy = s_xy[slot][1], slo = s_xy[slot][2];
+            xf = (float)(((sx >> L) + (uint32_t)(c & 1)) << L);
+            yf = (float)(slo + ((((sy - slo) >> L) + (uint32_t)(c >> 1)) << L));
+        }
+        float vd[F::NV];
+        get_v_data<F>(r, vb + (uint64_t)r.v[0] * F::NV, vb + (uint64_t)r.v[1] * F::NV, vb + (uint64_t)r.v[2] * F::NV,
+                      xf, yf, vd);
+        F::fragment(u, vd, s_frag[slot][c]);
+    }
+    __syncthreads();
+
+    // 4. combine (pipeline.rs:541-573) and store
+    if (!win) return;
+    float frag[F::NF];
+    if (L == 0) {
+#pragma unroll
+        for (int i = 0; i < F::NF; ++i) frag[i] = s_frag[tid][0][i];
+    } else {
+        int src[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            src[c] = (need & (1u << c)) ? tid : ((tid & ~31) | (lane & ~17) | (c & 1) | ((c >> 1) << 4));
+        const float div = 1.0f / (float)(1u << L);
+        const float fx = rfract((float)x * div);
+        const float fy = rfract((float)(y - lo) * div);
+#pragma unroll
+        for (int i = 0; i < F::NF; ++i) {
+            const float a0 = s_frag[src[0]][0][i] * (1.0f - fy) + s_frag[src[2]][2][i] * fy;
+            const float a1 = s_frag[src[1]][1][i] * (1.0f - fy) + s_frag[src[3]][3][i] * fy;
+            frag[i] = a0 * (1.0f - fx) + a1 * fx;
+        }
+    }
+    store_pixel<F>(s, x, y, frag);
 }
 
 }  // namespace eucg
