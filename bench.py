@@ -41,8 +41,18 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 N_SCENES = 256
-WORKLOAD = ("256 scenes, tris logU[100,1e5] (sphere/knot/soup), res U{64,128,256,512}^2, "
-            "50% Msaa{level:1}, 256^2 RGBA8 textures, textured Phong")
+# name -> (description, frames per step by default, unit)
+WORKLOADS = {
+    "batch": ("256 scenes, tris logU[100,1e5] (sphere/knot/soup), res U{64,128,256,512}^2, "
+              "50% Msaa{level:1}, 256^2 RGBA8 textures, textured Phong", N_SCENES, "scenes/s"),
+    "sphere": ("640x480 RGB8 + f32 depth, UV sphere 64x32 (3,968 tris), Gouraud, seeded rotation per frame, "
+               "LESS_WRITE, back-face culling", 1024, "frames/s"),
+    "soup": ("1920x1080 RGBA8 + f32 depth, 200k-triangle clip-space soup, areas logU[1,1e4] px, "
+             "per-vertex RGBA8, LESS_WRITE, permuted u32 indices", 1, "frames/s"),
+    "knot": ("two passes: 2048^2 f32 shadow map, then 1920x1080 RGBA8 textured Phong (1024^2 value noise, "
+             "tiled bilinear) with Msaa{level:1}; (2,3) torus knot, 500k tris", 4, "frames/s"),
+}
+WORKLOAD = WORKLOADS["batch"][0]
 
 
 def parse():
@@ -57,7 +67,14 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample budget")
     ap.add_argument("--only-batched", action="store_true",
                     help="run only the batched leg (no per-scene, e2e or CPU legs), e.g. under ncu")
-    return ap.parse_args()
+    ap.add_argument("--workload", default="batch", choices=sorted(WORKLOADS),
+                    help="batch: the 256 uneven scenes (default); sphere / soup / knot: the small plain, "
+                         "fill-rate and two-pass configurations, --frames of them per step")
+    ap.add_argument("--frames", type=int, default=0, help="frames per step for sphere/soup/knot (0 = default)")
+    args = ap.parse_args()
+    if args.workload != "batch":
+        args.scenes = args.frames or WORKLOADS[args.workload][1]
+    return args
 
 
 def dist_env():
@@ -69,7 +86,14 @@ def dist_env():
 
 def make_frames(args, rank):
     from euc_gb300 import scenes
-    return scenes.batch_frames(seed=args.seed + 1000 * rank, n=args.scenes)
+    seed = args.seed + 1000 * rank
+    if args.workload == "sphere":
+        return [scenes.sphere_frame(seed=seed + i) for i in range(args.scenes)]
+    if args.workload == "soup":
+        return [scenes.soup_frame(seed=seed + i) for i in range(args.scenes)]
+    if args.workload == "knot":
+        return [scenes.knot_frame(seed=seed + i) for i in range(args.scenes)]
+    return scenes.batch_frames(seed=seed, n=args.scenes)
 
 
 # ---------------------------------------------------------------------------
@@ -161,14 +185,15 @@ def run_reference(args):
         total_n += n
         total_t += t
     v = total_n / total_t
-    out = {"metric": "scenes/s (batched render, exact coverage)", "impl": "reference", "value": v,
-           "unit": "scenes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+    desc, _, unit = WORKLOADS[args.workload]
+    out = {"metric": "%s (batched render, exact coverage)" % unit, "impl": "reference", "value": v,
+           "unit": unit, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": 1e3 * total_t / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators)",
-           "config": {"workload": WORKLOAD, "scenes": args.scenes, "seed": args.seed},
-           "cpu_baseline": {"value": v, "unit": "scenes/s", "cores": threads, "kind": "port",
-                            "sample": "%d scenes (rotating through the 256) in %.1f s" % (total_n, total_t)},
-           "e2e": {"value": v, "unit": "scenes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "config": {"workload": desc, "name": args.workload, "scenes": args.scenes, "seed": args.seed},
+           "cpu_baseline": {"value": v, "unit": unit, "cores": threads, "kind": "port",
+                            "sample": "%d scenes (rotating through the %d) in %.1f s" % (total_n, len(frames), total_t)},
+           "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
 
@@ -260,8 +285,19 @@ def run_gpu(args):
     for _ in range(max(args.warmup, 3)):
         step()
     capi.check(ctx.sync(fr._stream_ptr(stream)), "warm-up")
-    st = ctx.stats(fr._stream_ptr(stream))
-    cand_per_step = st.candidates  # single-pass scenes: one batch call per step
+    # candidate fragments of one step, pass by pass (stats cover one batch call)
+    cand_per_step = 0
+    batch.clear()
+    npass = max(len(f.frame.passes) for f in batch.frames)
+    for k in range(npass):
+        scenes_k, keep = [], []
+        for df in batch.frames:
+            if k < len(df.frame.passes):
+                s, kp = df.scene(k)
+                scenes_k.append(s)
+                keep.append(kp)
+        capi.check(ctx.render_batch(scenes_k, fr._stream_ptr(stream)), "render_batch")
+        cand_per_step += ctx.stats(fr._stream_ptr(stream)).candidates
     ctx.profile()  # reset counters
 
     bus = None
@@ -323,19 +359,20 @@ def run_gpu(args):
     cpu = None
     if rank == 0 and not args.no_baseline and not args.only_batched:
         n, t, threads = cpu_sample(specs, args.cpu_seconds)
-        cpu = {"value": n / t, "unit": "scenes/s", "cores": threads, "kind": "port",
+        cpu = {"value": n / t, "unit": WORKLOADS[args.workload][2], "cores": threads, "kind": "port",
                "sample": "first %d of the %d scenes in %.1f s (oracle render_par, %d threads)" % (n, len(specs), t, threads)}
     if rank == 0:
+        desc, _, unit = WORKLOADS[args.workload]
         out = {
-            "metric": "scenes/s (batched render, exact coverage)", "value": value, "unit": "scenes/s",
+            "metric": "%s (batched render, exact coverage)" % unit, "value": value, "unit": unit,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generators), resident in HBM",
-            "config": {"workload": WORKLOAD, "scenes": args.scenes, "seed": args.seed,
+            "config": {"workload": desc, "name": args.workload, "scenes": args.scenes, "seed": args.seed,
                        "l2": "no flush: %.0f MB of inputs and targets per step > 129 MB L2" % (
                            (alg_bytes + 8 * sum(t.width * t.height for f in specs for t in f.targets if t.fmt != 4)) / 1e6),
                        "parallelism": "replicas" if world > 1 else "1 GPU"},
-            "per_scene": {"value": per_scene, "unit": "scenes/s", "path": "euc_render per scene"},
+            "per_scene": {"value": per_scene, "unit": unit, "path": "euc_render per scene"},
             "batched_speedup": value / world / per_scene if per_scene else None,
             "mfrag_per_s": cand_per_step * world / (ms_step / 1e3) / 1e6,
             "mtri_per_s": sum(f.ntris for f in specs) * world / (ms_step / 1e3) / 1e6,
@@ -344,8 +381,8 @@ def run_gpu(args):
             "roofline": {"bound": "hbm", "kernel": "k_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": alg_bytes,
-                         "traffic": traffic.get("k_" + dom) if traffic else None},
-            "e2e": {"value": e2e, "unit": "scenes/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                         "traffic": traffic.get(args.workload, {}).get("k_" + dom) if traffic else None},
+            "e2e": {"value": e2e, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "path": "euc_render_host per scene (host buffers, blocking)"},
             "cpu_baseline": cpu,
             "clocks": clk,

@@ -133,3 +133,7 @@ class Context:
     def render_batch(self, scenes, stream=None):
         arr = (abi.Scene * len(scenes))(*scenes)
         return lib().euc_render_batch(self.handle, arr, len(scenes), stream)
+
+    def render_scene_array(self, arr, stream=None):
+        """euc_render_batch on a prebuilt ctypes array of abi.Scene."""
+        return lib().euc_render_batch(self.handle, arr, len(arr), stream)

@@ -41,7 +41,7 @@ struct StageSlot {
 struct euc_ctx {
     int device = 0;
     int nsm = 0;
-    DevBuf clip, vdata, recs, rows, chunk_sums, live_tri, live_rowoff, totals, vbuf, err, stats;
+    DevBuf clip, vdata, recs, rows, chunk_sums, live_tri, live_rowoff, totals, vbuf, err, stats, cov;
     int raster_blocks = 0;  // resident k_raster blocks per SM
     // buffers used by euc_render_host
     DevBuf h_verts, h_idx, h_pixel, h_depth, h_tex[2];
@@ -278,6 +278,23 @@ int acquire_slot(euc_ctx *ctx, size_t bytes, StageSlot *&out) {
     return EUC_OK;
 }
 
+// Chunks per group of the chunk-group kernels (k_init, k_resolve): 1 while
+// the launch has fewer chunks than 16 blocks per SM can hold, growing to
+// kChunkGroup for large batches so that the scene search is amortised.
+uint32_t chunk_group(uint64_t nchunks, int nsm) {
+    const uint64_t slots = (uint64_t)(nsm > 0 ? nsm : 1) * 16;
+    return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(kChunkGroup, nchunks / slots));
+}
+
+// Grid of the chunk-group kernels: one block per group, at most 16 blocks per
+// SM (the blocks stride the groups).
+unsigned chunk_grid(uint64_t nchunks, int nsm) {
+    const uint32_t g = chunk_group(nchunks, nsm);
+    const uint64_t groups = (nchunks + g - 1) / g;
+    const uint64_t cap = (uint64_t)(nsm > 0 ? nsm : 1) * 16;
+    return (unsigned)std::max<uint64_t>(1, std::min(groups, cap));
+}
+
 // Resident blocks of k_raster per SM (its grid is persistent).
 int raster_blocks_per_sm() {
     static int n = 0;
@@ -319,8 +336,11 @@ template <class F>
 void launch_resolve(const SceneDev *sc, const uint64_t *pb, int s0, int s1, uint64_t blk0, uint64_t nblk, euc_ctx *ctx,
                     cudaStream_t st) {
     if (nblk)
-        k_resolve<F><<<(unsigned)nblk, kBlock, 0, st>>>(sc, pb, s0, s1, blk0, (const TriRec *)ctx->recs.p,
-                                                        (const float *)ctx->vdata.p, (const unsigned long long *)ctx->vbuf.p);
+        k_resolve<F><<<chunk_grid(nblk, ctx->nsm), kBlock, 0, st>>>(sc, pb, s0, s1, blk0, nblk,
+                                                                    chunk_group(nblk, ctx->nsm),
+                                                                    (const TriRec *)ctx->recs.p, (const float *)ctx->vdata.p,
+                                                                    (const unsigned long long *)ctx->vbuf.p,
+                                                                    (const uint4 *)ctx->cov.p);
 }
 
 void dispatch_vertex(uint32_t shader, const SceneDev *sc, const uint64_t *vb, int s0, int s1, uint64_t blk0, uint64_t nblk,
@@ -391,6 +411,7 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
     if ((rc = grow(ctx->vbuf, pix * sizeof(unsigned long long)))) return rc;
     if ((rc = grow(ctx->err, ns * sizeof(int)))) return rc;
     if ((rc = grow(ctx->stats, ns * sizeof(SceneStats)))) return rc;
+    if ((rc = grow(ctx->cov, ns * sizeof(uint4)))) return rc;
     // staging: scene table | vtx bases | tri bases | pix bases | uniforms
     const size_t off_sc = 0;
     const size_t off_vb = pad_up(ns * sizeof(SceneDev), 16);
@@ -425,6 +446,7 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
                    *dpb = (const uint64_t *)(dv + off_pb), *drb = (const uint64_t *)(dv + off_rb);
     CUDA_TRY(cudaMemsetAsync(ctx->err.p, 0, ns * sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(ctx->stats.p, 0, ns * sizeof(SceneStats), st));
+    CUDA_TRY(cudaMemsetAsync(ctx->cov.p, 0xFF, ns * sizeof(uint4), st));  // empty rectangles
     // vertex stage, one launch per shader kind
     cudaEvent_t e0 = prof_event(ctx, st);
     for (int a = 0; a < ns;) {
@@ -439,13 +461,15 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
     cudaEvent_t e1 = prof_event(ctx, st);
     k_setup<<<(unsigned)nchunks, kBlock, 0, st>>>(dsc, dtb, ns, (const float4 *)ctx->clip.p, (TriRec *)ctx->recs.p,
                                                    (uint32_t *)ctx->rows.p, (uint2 *)ctx->chunk_sums.p, (int *)ctx->err.p,
-                                                   (SceneStats *)ctx->stats.p);
+                                                   (SceneStats *)ctx->stats.p, (uint4 *)ctx->cov.p);
     cudaEvent_t e2 = prof_event(ctx, st);
     k_scan<<<(unsigned)nscan, kBlock, 0, st>>>((const uint32_t *)ctx->rows.p, (const uint2 *)ctx->chunk_sums.p, tri,
                                                (uint32_t *)ctx->live_tri.p, (uint64_t *)ctx->live_rowoff.p,
                                                (unsigned long long *)ctx->totals.p);
     cudaEvent_t e3 = prof_event(ctx, st);
-    k_init<<<(unsigned)(pix / kBlock), kBlock, 0, st>>>(dsc, dpb, ns, (unsigned long long *)ctx->vbuf.p);
+    k_init<<<chunk_grid(pix / kBlock, ctx->nsm), kBlock, 0, st>>>(dsc, dpb, ns, (const uint4 *)ctx->cov.p,
+                                                                   (unsigned long long *)ctx->vbuf.p, pix / kBlock,
+                                                                   chunk_group(pix / kBlock, ctx->nsm));
     cudaEvent_t e4 = prof_event(ctx, st);
     k_raster<<<(unsigned)(ctx->nsm * ctx->raster_blocks), kBlock, 0, st>>>(
         dsc, (const TriRec *)ctx->recs.p, (const uint32_t *)ctx->live_tri.p, (const uint64_t *)ctx->live_rowoff.p,
@@ -521,7 +545,7 @@ int euc_ctx_destroy(euc_ctx *ctx) {
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
     DevBuf *bufs[] = {&ctx->clip, &ctx->vdata, &ctx->recs, &ctx->rows, &ctx->chunk_sums, &ctx->live_tri, &ctx->live_rowoff,
-                      &ctx->totals, &ctx->vbuf, &ctx->err, &ctx->stats, &ctx->h_verts,
+                      &ctx->totals, &ctx->vbuf, &ctx->err, &ctx->stats, &ctx->cov, &ctx->h_verts,
                       &ctx->h_idx, &ctx->h_pixel, &ctx->h_depth, &ctx->h_tex[0], &ctx->h_tex[1]};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
@@ -553,6 +577,7 @@ int euc_ctx_reserve(euc_ctx *ctx, uint64_t max_verts, uint64_t max_tris, uint64_
     if ((rc = grow(ctx->vbuf, pix * sizeof(unsigned long long)))) return rc;
     if ((rc = grow(ctx->err, ns * sizeof(int)))) return rc;
     if ((rc = grow(ctx->stats, ns * sizeof(SceneStats)))) return rc;
+    if ((rc = grow(ctx->cov, ns * sizeof(uint4)))) return rc;
     return EUC_OK;
 }
 
@@ -765,6 +790,7 @@ constexpr size_t kNaStage = 4096;  // scene table, bases, uniforms
 constexpr size_t kNaOffErr = kNaStage;
 constexpr size_t kNaOffStats = kNaOffErr + 256;
 constexpr size_t kNaOffTotals = kNaOffStats + 256;
+constexpr size_t kNaOffCov = kNaOffTotals + 64;  // inside the 256-byte totals region
 constexpr size_t kNaOffClip = kNaOffTotals + 256;
 constexpr size_t kNaOffVdata = kNaOffClip + kNaMaxVerts * sizeof(float4);
 constexpr size_t kNaOffRecs = kNaOffVdata + kNaMaxVerts * kNaMaxNV * sizeof(float);
@@ -816,6 +842,8 @@ int na_scratch(int dev, unsigned char **ptr, int *nsm) {
     return EUC_OK;
 }
 
+thread_local int t_na_nsm = 1;  // SM count of the device of the current call
+
 template <class F>
 void na_vertex_resolve(bool vertex, const SceneDev *sc, const uint64_t *base, uint64_t nblk, unsigned char *a,
                        cudaStream_t st) {
@@ -824,9 +852,11 @@ void na_vertex_resolve(bool vertex, const SceneDev *sc, const uint64_t *base, ui
         k_vertex<F><<<(unsigned)nblk, kBlock, 0, st>>>(sc, base, 0, 1, 0, (float4 *)(a + kNaOffClip),
                                                        (float *)(a + kNaOffVdata));
     else
-        k_resolve<F><<<(unsigned)nblk, kBlock, 0, st>>>(sc, base, 0, 1, 0, (const TriRec *)(a + kNaOffRecs),
-                                                        (const float *)(a + kNaOffVdata),
-                                                        (const unsigned long long *)(a + kNaOffVbuf));
+        k_resolve<F><<<chunk_grid(nblk, t_na_nsm), kBlock, 0, st>>>(sc, base, 0, 1, 0, nblk,
+                                                                    chunk_group(nblk, t_na_nsm), (const TriRec *)(a + kNaOffRecs),
+                                                               (const float *)(a + kNaOffVdata),
+                                                               (const unsigned long long *)(a + kNaOffVbuf),
+                                                               (const uint4 *)(a + kNaOffCov));
 }
 
 void na_dispatch(bool vertex, uint32_t shader, const SceneDev *sc, const uint64_t *base, uint64_t nblk,
@@ -896,15 +926,19 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
     const uint64_t *zero_base = (const uint64_t *)(a + off_b);  // every base is 0 for a single scene
     CUDA_TRY(cudaMemsetAsync(a + kNaOffErr, 0, sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(a + kNaOffStats, 0, sizeof(SceneStats), st));
+    CUDA_TRY(cudaMemsetAsync(a + kNaOffCov, 0xFF, sizeof(uint4), st));
+    t_na_nsm = nsm;
     na_dispatch(true, d.shader, dsc, zero_base, vtx / kBlock, a, st);
     k_setup<<<(unsigned)(tri / kBlock), kBlock, 0, st>>>(dsc, zero_base, 1, (const float4 *)(a + kNaOffClip),
                                                           (TriRec *)(a + kNaOffRecs), (uint32_t *)(a + kNaOffRows),
                                                           (uint2 *)(a + kNaOffChunks), (int *)(a + kNaOffErr),
-                                                          (SceneStats *)(a + kNaOffStats));
+                                                          (SceneStats *)(a + kNaOffStats), (uint4 *)(a + kNaOffCov));
     k_scan<<<(unsigned)((tri + kScanBlock - 1) / kScanBlock), kBlock, 0, st>>>(
         (const uint32_t *)(a + kNaOffRows), (const uint2 *)(a + kNaOffChunks), tri, (uint32_t *)(a + kNaOffLiveTri),
         (uint64_t *)(a + kNaOffLiveOff), (unsigned long long *)(a + kNaOffTotals));
-    k_init<<<(unsigned)(pix / kBlock), kBlock, 0, st>>>(dsc, zero_base, 1, (unsigned long long *)(a + kNaOffVbuf));
+    k_init<<<chunk_grid(pix / kBlock, nsm), kBlock, 0, st>>>(dsc, zero_base, 1, (const uint4 *)(a + kNaOffCov),
+                                                              (unsigned long long *)(a + kNaOffVbuf), pix / kBlock,
+                                                              chunk_group(pix / kBlock, nsm));
     k_raster<<<(unsigned)(nsm * raster_blocks_per_sm()), kBlock, 0, st>>>(
         dsc, (const TriRec *)(a + kNaOffRecs), (const uint32_t *)(a + kNaOffLiveTri), (const uint64_t *)(a + kNaOffLiveOff),
         (unsigned long long *)(a + kNaOffTotals), (const int *)(a + kNaOffErr),

@@ -182,7 +182,8 @@ __global__ void __launch_bounds__(kBlock) k_vertex(const SceneDev *__restrict__ 
 __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ tri_base,
                                                   int nsc, const float4 *__restrict__ clip, TriRec *__restrict__ recs,
                                                   uint32_t *__restrict__ rows, uint2 *__restrict__ chunk_sums,
-                                                  int *__restrict__ err, SceneStats *__restrict__ stats) {
+                                                  int *__restrict__ err, SceneStats *__restrict__ stats,
+                                                  uint4 *__restrict__ cov) {
     __shared__ int s_scene;
     __shared__ uint32_t s_red[2][kBlock / 32];
     const uint64_t t = (uint64_t)blockIdx.x * kBlock + threadIdx.x;
@@ -192,6 +193,8 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
     const SceneDev &s = sc[si];
     const uint64_t lt = t - s.tri_base;
     uint32_t nrows = 0, culled = 0;
+    // pixels this primitive may touch: x in [cx0, cx1), y in [cy0, cy1)
+    uint32_t cx0 = 0xFFFFFFFFu, cy0 = 0xFFFFFFFFu, cx1 = 0, cy1 = 0;
     if (lt < s.ngroups) {
         uint32_t vid[3] = {0, 0, 0};
         bool ok = true;
@@ -322,10 +325,27 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
 #pragma unroll
                 for (int k = 0; k < 8; ++k) dst[k] = src[k];
                 nrows = bx1 > bx0 ? by1 - by0 : 0u;
+                if (nrows) {
+                    cx0 = bx0;
+                    cx1 = bx1;
+                    cy0 = by0;
+                    cy1 = by1;
+                }
             }
         }
     }
     rows[t] = nrows;
+    // the scene's covered rectangle: min of (x0, y0, ~x1, ~y1) over its primitives
+    {
+        const uint32_t m0 = __reduce_min_sync(0xFFFFFFFFu, cx0), m1 = __reduce_min_sync(0xFFFFFFFFu, cy0);
+        const uint32_t m2 = __reduce_min_sync(0xFFFFFFFFu, ~cx1), m3 = __reduce_min_sync(0xFFFFFFFFu, ~cy1);
+        if ((threadIdx.x & 31) == 0 && m0 != 0xFFFFFFFFu) {
+            atomicMin(&cov[si].x, m0);
+            atomicMin(&cov[si].y, m1);
+            atomicMin(&cov[si].z, m2);
+            atomicMin(&cov[si].w, m3);
+        }
+    }
     // per-block sums for the scan, and the culled count of this scene
     const uint32_t live = nrows ? 1u : 0u;
     uint32_t wl = warp_sum(live), wr = warp_sum(nrows), wc = warp_sum(culled);
@@ -398,24 +418,60 @@ __global__ void __launch_bounds__(kBlock) k_scan(const uint32_t *__restrict__ ro
 }
 
 // ---------------------------------------------------------------------------
-// k_init: visibility key of every pixel before rasterisation.
+// k_init: visibility key of every pixel that a primitive may touch (the
+// scene's covered rectangle); pixels outside it are never read or written.
 // ---------------------------------------------------------------------------
+EUC_DEV bool covered(const uint4 &c, uint32_t x, uint32_t y) {
+    return x >= c.x && y >= c.y && x < ~c.z && y < ~c.w;
+}
+
+// Blocks of k_init / k_resolve walk groups of `group` consecutive 256-pixel
+// chunks, grid-strided, so the scene table is searched once per group rather
+// than once per chunk (the host picks group = 1 for small launches, up to
+// kChunkGroup for large batches).
+constexpr int kChunkGroup = 16;
+
+// Rows [y0, y1] of the pixels q0 .. q0+255 of a W-wide scene do not meet the
+// covered rectangle: the whole chunk can be skipped.
+EUC_DEV bool chunk_outside(const uint4 &c, uint64_t q0, uint32_t W) {
+    const uint64_t y0 = q0 / W, y1 = (q0 + kBlock - 1) / W;
+    return y1 < c.y || y0 >= ~c.w;
+}
+
+// Scene of chunk `c` given the scene of an earlier chunk of the same group.
+EUC_DEV int advance_scene(const uint64_t *base, int nsc, int si, uint64_t c) {
+    while (si + 1 < nsc && base[si + 1] <= c) ++si;
+    return si;
+}
+
 __global__ void __launch_bounds__(kBlock) k_init(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ pix_base,
-                                                 int nsc, unsigned long long *__restrict__ vbuf) {
+                                                 int nsc, const uint4 *__restrict__ cov,
+                                                 unsigned long long *__restrict__ vbuf, uint64_t nchunks,
+                                                 uint32_t group) {
     __shared__ int s_scene;
-    const uint64_t pos = (uint64_t)blockIdx.x * kBlock;
-    if (threadIdx.x == 0) s_scene = find_scene(pix_base, nsc, pos);
-    __syncthreads();
-    const SceneDev &s = sc[s_scene];
-    const uint64_t q = pos + threadIdx.x - s.pix_base;
-    if (q >= (uint64_t)s.W * s.H) return;
-    unsigned long long key = ~0ull;
-    if (s.keytype == KEY_MIN) {
-        const uint32_t x = (uint32_t)(q % s.W), y = (uint32_t)(q / s.W);
-        const float d0 = *reinterpret_cast<const float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x);
-        key = init_key_min(d0, s.depth_test == EUC_TEST_GREATER);
+    for (uint64_t g = blockIdx.x; g * group < nchunks; g += gridDim.x) {
+        const uint64_t c0 = g * group;
+        __syncthreads();
+        if (threadIdx.x == 0) s_scene = find_scene(pix_base, nsc, c0 * kBlock);
+        __syncthreads();
+        int si = s_scene;
+        for (uint64_t c = c0; c < c0 + group && c < nchunks; ++c) {
+            const uint64_t pos = c * kBlock;
+            si = advance_scene(pix_base, nsc, si, pos);
+            const SceneDev &s = sc[si];
+            if (chunk_outside(cov[si], pos - s.pix_base, s.W)) continue;
+            const uint64_t q = pos + threadIdx.x - s.pix_base;
+            if (q >= (uint64_t)s.W * s.H) continue;
+            const uint32_t x = (uint32_t)(q % s.W), y = (uint32_t)(q / s.W);
+            if (!covered(cov[si], x, y)) continue;
+            unsigned long long key = ~0ull;
+            if (s.keytype == KEY_MIN) {
+                const float d0 = *reinterpret_cast<const float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x);
+                key = init_key_min(d0, s.depth_test == EUC_TEST_GREATER);
+            }
+            vbuf[s.pix_base + q] = key;
+        }
     }
-    vbuf[s.pix_base + q] = key;
 }
 
 // ---------------------------------------------------------------------------
@@ -671,16 +727,19 @@ __host__ __device__ inline uint64_t resolve_blocks(const SceneDev &s) {
 }
 
 template <class F>
-__global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ res_base,
-                                                    int s_begin, int s_end, uint64_t blk_begin,
-                                                    const TriRec *__restrict__ recs, const float *__restrict__ vdata,
-                                                    const unsigned long long *__restrict__ vbuf) {
-    __shared__ int s_scene;
-    const uint64_t blk = blk_begin + blockIdx.x;
-    if (threadIdx.x == 0) s_scene = s_begin + find_scene(res_base + s_begin, s_end - s_begin, blk);
-    __syncthreads();
-    const SceneDev &s = sc[s_scene];
-    const uint64_t lb = blk - res_base[s_scene];
+struct ResolveSmem {
+    uint32_t t[kBlock];
+    uint32_t xy[kBlock][3];
+    uint16_t job[4 * kBlock];
+    float frag[kBlock][4][F::NF];
+    uint32_t scan[kBlock / 32 + 1];
+};
+
+// One 256-pixel chunk `lb` of scene `s`; every thread of the block calls it.
+template <class F>
+EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, const TriRec *__restrict__ recs,
+                           const float *__restrict__ vdata, const unsigned long long *__restrict__ vbuf,
+                           ResolveSmem<F> &sm) {
     const int tid = threadIdx.x, lane = tid & 31;
     // 1. this thread's pixel
     uint32_t x = 0, y = 0, lo = 0;
@@ -707,24 +766,25 @@ __global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__
             lo = (y / s.gr) * s.gr;
         }
     }
+    inside = inside && covered(cv, x, y);  // no primitive reaches other pixels
     uint32_t t = 0xFFFFFFFFu;
     float z = 0.0f;
     const bool win = inside && decode_key(s, vbuf[s.pix_base + (uint64_t)y * s.W + x], t, z);
     if (win && s.depth_write) *reinterpret_cast<float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x) = z;
     if (!s.pixel_write) return;  // uniform over the block (one scene)
+    if (!__syncthreads_or(win)) return;  // nothing to shade in this chunk
 
-    // 2. the fragment evaluations this block needs, compacted into a job list.
+    // 2. the fragment evaluations this chunk needs, compacted into a job list.
     // A job is (pixel slot, corner); corner 0 is the pixel itself when there
     // is no MSAA.  With level-1 MSAA each pixel shades the corner of its 2x2
     // cell at its own offset and reuses the other three from the cell's other
     // pixels when they have the same winner.  A coarse fragment is a pure
     // function of (primitive, grid point), so sharing changes no bits (euc's
     // own coarse cache, pipeline.rs:477-494, is transparent the same way).
-    __shared__ uint32_t s_t[kBlock];
-    __shared__ uint32_t s_xy[kBlock][3];
-    __shared__ uint16_t s_job[4 * kBlock];
-    __shared__ float s_frag[kBlock][4][F::NF];
-    __shared__ uint32_t s_scan[kBlock / 32 + 1];
+    uint32_t *s_t = sm.t;
+    uint32_t(*s_xy)[3] = sm.xy;
+    uint16_t *s_job = sm.job;
+    float(*s_frag)[4][F::NF] = sm.frag;
     s_t[tid] = win ? t : 0xFFFFFFFFu;
     s_xy[tid][0] = x;
     s_xy[tid][1] = y;
@@ -746,7 +806,7 @@ __global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__
         }
     }
     uint32_t njobs;
-    uint32_t off = block_excl_scan<uint32_t>(__popc(need), s_scan, &njobs);
+    uint32_t off = block_excl_scan<uint32_t>(__popc(need), sm.scan, &njobs);
 #pragma unroll
     for (int c = 0; c < 4; ++c)
         if (need & (1u << c)) s_job[off++] = (uint16_t)((tid << 2) | c);
@@ -797,6 +857,37 @@ __global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__
         }
     }
     store_pixel<F>(s, x, y, frag);
+}
+
+// Blocks walk groups of kChunkGroup chunks (grid-strided); the chunk of each
+// scene are [res_base[s], res_base[s] + resolve_blocks(s)).
+template <class F>
+__global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ res_base,
+                                                    int s_begin, int s_end, uint64_t blk_begin, uint64_t nblk,
+                                                    uint32_t group, const TriRec *__restrict__ recs,
+                                                    const float *__restrict__ vdata,
+                                                    const unsigned long long *__restrict__ vbuf,
+                                                    const uint4 *__restrict__ cov) {
+    __shared__ ResolveSmem<F> sm;
+    __shared__ int s_scene;
+    const uint64_t *base = res_base + s_begin;
+    const int n = s_end - s_begin;
+    for (uint64_t g = blockIdx.x; g * group < nblk; g += gridDim.x) {
+        const uint64_t c0 = blk_begin + g * group;
+        __syncthreads();
+        if (threadIdx.x == 0) s_scene = find_scene(base, n, c0);
+        __syncthreads();
+        int si = s_scene;
+        for (uint64_t c = c0; c < c0 + group && c < blk_begin + nblk; ++c) {
+            si = advance_scene(base, n, si, c);
+            const SceneDev &s = sc[s_begin + si];
+            const uint4 cv = cov[s_begin + si];
+            const uint64_t lb = c - base[si];
+            if (!resolve_by_quads(s) && chunk_outside(cv, lb * kBlock, s.W)) continue;  // uniform
+            resolve_chunk<F>(s, cv, lb, recs, vdata, vbuf, sm);
+            __syncthreads();  // the next chunk reuses shared memory
+        }
+    }
 }
 
 }  // namespace eucg

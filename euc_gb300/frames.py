@@ -175,6 +175,24 @@ class DeviceBatch:
         self.color.zero_()
         self.depth.fill_(self.depth_clear)
 
+    def scene_arrays(self):
+        """Per pass k, a ctypes array of the euc_scene of every frame that has
+        a pass k.  Built once: the device pointers do not change between
+        renders, so repeated renders pay no per-scene host work."""
+        if getattr(self, "_arrays", None) is None:
+            npass = max(len(f.frame.passes) for f in self.frames)
+            arrays, keep = [], []
+            for k in range(npass):
+                scenes = []
+                for f in self.frames:
+                    if k < len(f.frame.passes):
+                        s, kp = f.scene(k)
+                        scenes.append(s)
+                        keep.append(kp)
+                arrays.append((abi.Scene * len(scenes))(*scenes))
+            self._arrays, self._keep = arrays, keep
+        return self._arrays
+
 
 def render_frame(ctx, dframe, stream=None, clear=True):
     """Clears the targets (if asked) and runs every pass with euc_render."""
@@ -200,7 +218,10 @@ def render_batch(ctx, dframes, stream=None, clear=True):
     if isinstance(dframes, DeviceBatch):
         if clear:
             dframes.clear()
-        dframes = dframes.frames
+        sp = _stream_ptr(stream)
+        for k, arr in enumerate(dframes.scene_arrays()):
+            capi.check(ctx.render_scene_array(arr, sp), "euc_render_batch(pass %d)" % k)
+        return
     elif clear:
         for f in dframes:
             f.clear()
