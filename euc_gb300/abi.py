@@ -38,6 +38,7 @@ WRAP_NONE, WRAP_CLAMP, WRAP_TILE, WRAP_MIRROR = 0, 1, 2, 3
 BANDS_PAR = 0
 BANDS_SEQ = 0xFFFFFFFF
 FLAG_PAR_EMPTY = 1
+FLAG_ORDERED = 2
 
 STAGE_NAMES = ("vertex", "setup", "scan", "init", "raster", "resolve")
 STAGE_COUNT = len(STAGE_NAMES)

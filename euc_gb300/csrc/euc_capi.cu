@@ -42,6 +42,7 @@ struct euc_ctx {
     int device = 0;
     int nsm = 0;
     DevBuf clip, vdata, recs, rows, chunk_sums, live_tri, live_rowoff, totals, vbuf, err, stats, cov;
+    DevBuf obsum, frags;  // ordered path: pixel-scan block sums, fragment lists
     int raster_blocks = 0;  // resident k_raster blocks per SM
     // buffers used by euc_render_host
     DevBuf h_verts, h_idx, h_pixel, h_depth, h_tex[2];
@@ -150,7 +151,7 @@ int plan_scene(const euc_scene &sc, Plan &p) {
     const euc_pipeline_desc &d = sc.desc;
     if (d.shader >= EUC_SHADER_COUNT) return EUC_ERR_INVALID;
     if (d.depth_test > EUC_TEST_GREATER || d.cull > EUC_CULL_FRONT || d.y_axis > EUC_Y_UP) return EUC_ERR_INVALID;
-    if (d.blend != EUC_BLEND_REPLACE) return EUC_ERR_INVALID;  // order-dependent blends: not in this path
+    if (d.blend > EUC_BLEND_ALPHA) return EUC_ERR_INVALID;
     const size_t need = uniforms_size_for(d.shader);
     if (!sc.uniforms || sc.uniforms_size < need) return EUC_ERR_INVALID;
     const euc_vertex_layout &l = sc.layout;
@@ -218,6 +219,7 @@ int plan_scene(const euc_scene &sc, Plan &p) {
         if (gr > H) gr = H > 0 ? H : 1;
     }
     if (W == 0 || H == 0) { p.skip = true; return EUC_OK; }
+    if ((uint64_t)W * H >= 0xFFFFFF00ull) return EUC_ERR_CAPACITY;  // pixel indices are 32-bit on the device
     const uint64_t nstream = sc.indices ? sc.nindices : sc.nverts;
     if (sc.nverts >= 0xFFFFFFFFull || nstream / 3 >= 0x3FFFFFFFull) return EUC_ERR_INVALID;
     SceneDev &s = p.d;
@@ -250,6 +252,10 @@ int plan_scene(const euc_scene &sc, Plan &p) {
     if (!s.pixel_write && !s.depth_write) { p.skip = true; return EUC_OK; }  // nothing is ever written
     if (s.pixel_write && px_empty) s.pixel_write = 0;  // Empty drops writes (texture.rs:315-318)
     s.keytype = (s.depth_write && (d.depth_test == EUC_TEST_LESS || d.depth_test == EUC_TEST_GREATER)) ? KEY_MIN : KEY_LAST;
+    // blends that read the old pixel depend on the order of every passing
+    // fragment: those scenes (and any with EUC_FLAG_ORDERED) replay per-pixel
+    // fragment lists instead of reducing visibility keys
+    if ((s.pixel_write && d.blend == EUC_BLEND_ALPHA) || (d.flags & EUC_FLAG_ORDERED)) s.keytype = KEY_ORDERED;
     p.nv = (uint32_t)shader_nv(d.shader);
     p.uniforms = sc.uniforms;
     p.usize = need;
@@ -367,6 +373,28 @@ void dispatch_resolve(uint32_t shader, const SceneDev *sc, const uint64_t *pb, i
     }
 }
 
+template <class F>
+void launch_resolve_ordered(const SceneDev *sc, const uint64_t *pb, int s0, int s1, uint64_t blk0, uint64_t nblk,
+                            euc_ctx *ctx, cudaStream_t st) {
+    if (nblk)
+        k_resolve_ordered<F><<<(unsigned)nblk, kBlock, 0, st>>>(sc, pb, s0, s1, blk0, (const TriRec *)ctx->recs.p,
+                                                                (const float *)ctx->vdata.p,
+                                                                (const unsigned long long *)ctx->vbuf.p,
+                                                                (const uint2 *)ctx->frags.p, (const uint4 *)ctx->cov.p);
+}
+
+void dispatch_resolve_ordered(uint32_t shader, const SceneDev *sc, const uint64_t *pb, int s0, int s1, uint64_t blk0,
+                              uint64_t nblk, euc_ctx *ctx, cudaStream_t st) {
+    switch (shader) {
+    case EUC_SHADER_FLAT: launch_resolve_ordered<FlatFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_VCOLOR: launch_resolve_ordered<VColorFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_GOURAUD: launch_resolve_ordered<GouraudFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_TEXTURED: launch_resolve_ordered<TexturedFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_PHONG: launch_resolve_ordered<PhongFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_SHADOW: launch_resolve_ordered<ShadowFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
+    }
+}
+
 // Runs a batch of scenes.  All pointers inside `scenes` are device pointers.
 int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) {
     std::vector<Plan> plans;
@@ -379,7 +407,12 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
     ctx->last_nscenes = (int)plans.size();
     if (plans.empty()) return EUC_OK;
     // group scenes by shader kind so that each kind owns contiguous ranges
-    std::stable_sort(plans.begin(), plans.end(), [](const Plan &a, const Plan &b) { return a.d.shader < b.d.shader; });
+    // group scenes by (ordered path, shader kind): each group owns contiguous
+    // vertex / pixel / resolve ranges, and ordered scenes come last so that
+    // their pixels form one range for the pixel scan
+    auto group_of = [](const Plan &p) { return (p.d.keytype == KEY_ORDERED ? 64u : 0u) + p.d.shader; };
+    std::stable_sort(plans.begin(), plans.end(),
+                     [&](const Plan &a, const Plan &b) { return group_of(a) < group_of(b); });
     const int ns = (int)plans.size();
     uint64_t vtx = 0, vd = 0, tri = 0, pix = 0, res = 0;
     std::vector<uint64_t> res_base(ns);
@@ -407,7 +440,7 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
     if ((rc = grow(ctx->chunk_sums, nchunks * sizeof(uint2)))) return rc;
     if ((rc = grow(ctx->live_tri, tri * sizeof(uint32_t)))) return rc;
     if ((rc = grow(ctx->live_rowoff, tri * sizeof(uint64_t)))) return rc;
-    if ((rc = grow(ctx->totals, 4 * sizeof(unsigned long long)))) return rc;
+    if ((rc = grow(ctx->totals, 8 * sizeof(unsigned long long)))) return rc;
     if ((rc = grow(ctx->vbuf, pix * sizeof(unsigned long long)))) return rc;
     if ((rc = grow(ctx->err, ns * sizeof(int)))) return rc;
     if ((rc = grow(ctx->stats, ns * sizeof(SceneStats)))) return rc;
@@ -471,18 +504,46 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
                                                                    (unsigned long long *)ctx->vbuf.p, pix / kBlock,
                                                                    chunk_group(pix / kBlock, ctx->nsm));
     cudaEvent_t e4 = prof_event(ctx, st);
-    k_raster<<<(unsigned)(ctx->nsm * ctx->raster_blocks), kBlock, 0, st>>>(
-        dsc, (const TriRec *)ctx->recs.p, (const uint32_t *)ctx->live_tri.p, (const uint64_t *)ctx->live_rowoff.p,
-        (unsigned long long *)ctx->totals.p, (const int *)ctx->err.p,
-                                                           (unsigned long long *)ctx->vbuf.p, (SceneStats *)ctx->stats.p);
-    cudaEvent_t e5 = prof_event(ctx, st);
+    const unsigned rgrid = (unsigned)(ctx->nsm * ctx->raster_blocks);
+    k_raster<<<rgrid, kBlock, 0, st>>>(dsc, (const TriRec *)ctx->recs.p, (const uint32_t *)ctx->live_tri.p,
+                                       (const uint64_t *)ctx->live_rowoff.p, (unsigned long long *)ctx->totals.p,
+                                       (const int *)ctx->err.p, (unsigned long long *)ctx->vbuf.p,
+                                       (SceneStats *)ctx->stats.p, 0, nullptr);
     ctx->launches += 4;
+    // ordered scenes: scan the per-pixel counts, size the fragment buffer
+    // (one stream synchronisation), fill the lists in a second raster pass
+    int first_ordered = ns;
+    while (first_ordered > 0 && plans[first_ordered - 1].d.keytype == KEY_ORDERED) --first_ordered;
+    if (first_ordered < ns) {
+        const uint64_t p0 = plans[first_ordered].d.pix_base, p1 = pix;
+        const uint64_t nb = (p1 - p0 + kOScanBlock - 1) / kOScanBlock;
+        if ((rc = grow(ctx->obsum, nb * sizeof(unsigned long long)))) return rc;
+        unsigned long long *totals = (unsigned long long *)ctx->totals.p;
+        k_oscan_reduce<<<(unsigned)nb, kBlock, 0, st>>>((const unsigned long long *)ctx->vbuf.p, p0, p1,
+                                                        (unsigned long long *)ctx->obsum.p);
+        k_oscan_apply<<<(unsigned)nb, kBlock, 0, st>>>((unsigned long long *)ctx->vbuf.p, p0, p1,
+                                                       (const unsigned long long *)ctx->obsum.p, totals + 4);
+        unsigned long long nfrag = 0;
+        CUDA_TRY(cudaMemcpyAsync(&nfrag, totals + 4, sizeof(nfrag), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        if (nfrag >= 0xFFFFFFFFull) return EUC_ERR_CAPACITY;  // list offsets are 32-bit
+        if ((rc = grow(ctx->frags, std::max<uint64_t>(nfrag, 1) * sizeof(uint2)))) return rc;
+        k_raster<<<rgrid, kBlock, 0, st>>>(dsc, (const TriRec *)ctx->recs.p, (const uint32_t *)ctx->live_tri.p,
+                                           (const uint64_t *)ctx->live_rowoff.p, (unsigned long long *)ctx->totals.p,
+                                           (const int *)ctx->err.p, (unsigned long long *)ctx->vbuf.p,
+                                           (SceneStats *)ctx->stats.p, 1, (uint2 *)ctx->frags.p);
+        ctx->launches += 3;
+    }
+    cudaEvent_t e5 = prof_event(ctx, st);
     for (int a = 0; a < ns;) {
         int b = a;
-        while (b < ns && plans[b].d.shader == plans[a].d.shader) ++b;
+        while (b < ns && group_of(plans[b]) == group_of(plans[a])) ++b;
         const uint64_t blk0 = res_base[a];
         const uint64_t blk1 = b < ns ? res_base[b] : res;
-        dispatch_resolve(plans[a].d.shader, dsc, drb, a, b, blk0, blk1 - blk0, ctx, st);
+        if (plans[a].d.keytype == KEY_ORDERED)
+            dispatch_resolve_ordered(plans[a].d.shader, dsc, drb, a, b, blk0, blk1 - blk0, ctx, st);
+        else
+            dispatch_resolve(plans[a].d.shader, dsc, drb, a, b, blk0, blk1 - blk0, ctx, st);
         ctx->launches += blk1 > blk0;
         a = b;
     }
@@ -545,7 +606,8 @@ int euc_ctx_destroy(euc_ctx *ctx) {
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
     DevBuf *bufs[] = {&ctx->clip, &ctx->vdata, &ctx->recs, &ctx->rows, &ctx->chunk_sums, &ctx->live_tri, &ctx->live_rowoff,
-                      &ctx->totals, &ctx->vbuf, &ctx->err, &ctx->stats, &ctx->cov, &ctx->h_verts,
+                      &ctx->totals, &ctx->vbuf, &ctx->err, &ctx->stats, &ctx->cov, &ctx->obsum, &ctx->frags,
+                      &ctx->h_verts,
                       &ctx->h_idx, &ctx->h_pixel, &ctx->h_depth, &ctx->h_tex[0], &ctx->h_tex[1]};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
@@ -573,7 +635,7 @@ int euc_ctx_reserve(euc_ctx *ctx, uint64_t max_verts, uint64_t max_tris, uint64_
     if ((rc = grow(ctx->chunk_sums, (tri / kBlock + 1) * sizeof(uint2)))) return rc;
     if ((rc = grow(ctx->live_tri, tri * sizeof(uint32_t)))) return rc;
     if ((rc = grow(ctx->live_rowoff, tri * sizeof(uint64_t)))) return rc;
-    if ((rc = grow(ctx->totals, 4 * sizeof(unsigned long long)))) return rc;
+    if ((rc = grow(ctx->totals, 8 * sizeof(unsigned long long)))) return rc;
     if ((rc = grow(ctx->vbuf, pix * sizeof(unsigned long long)))) return rc;
     if ((rc = grow(ctx->err, ns * sizeof(int)))) return rc;
     if ((rc = grow(ctx->stats, ns * sizeof(SceneStats)))) return rc;
@@ -903,6 +965,9 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
         if (device_status) CUDA_TRY(cudaMemsetAsync(device_status, 0, sizeof(int), st));
         return EUC_OK;
     }
+    // order-dependent blends keep every fragment in lists whose size is only
+    // known on the device; they need euc_render's growable buffers
+    if (p.d.keytype == KEY_ORDERED) return EUC_ERR_CAPACITY;
     if (p.d.nverts > kNaMaxVerts || p.d.ngroups > kNaMaxGroups || (uint64_t)p.d.W * p.d.H > kNaMaxPixels ||
         p.nv > (uint32_t)kNaMaxNV)
         return EUC_ERR_CAPACITY;
@@ -942,7 +1007,7 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
     k_raster<<<(unsigned)(nsm * raster_blocks_per_sm()), kBlock, 0, st>>>(
         dsc, (const TriRec *)(a + kNaOffRecs), (const uint32_t *)(a + kNaOffLiveTri), (const uint64_t *)(a + kNaOffLiveOff),
         (unsigned long long *)(a + kNaOffTotals), (const int *)(a + kNaOffErr),
-        (unsigned long long *)(a + kNaOffVbuf), (SceneStats *)(a + kNaOffStats));
+        (unsigned long long *)(a + kNaOffVbuf), (SceneStats *)(a + kNaOffStats), 0, nullptr);
     na_dispatch(false, d.shader, dsc, zero_base, resolve_blocks(d), a, st);
     if (device_status)
         CUDA_TRY(cudaMemcpyAsync(device_status, a + kNaOffErr, sizeof(int), cudaMemcpyDeviceToDevice, st));

@@ -38,7 +38,10 @@ constexpr int kBlock = 256;           // threads per block in every kernel
 constexpr int kScanPer = 8;           // primitives per thread in k_scan
 constexpr int kScanBlock = kBlock * kScanPer;
 
-enum KeyType : uint32_t { KEY_NONE = 0, KEY_MIN = 1, KEY_LAST = 2 };
+// KEY_MIN / KEY_LAST: order-independent visibility keys (see above).
+// KEY_ORDERED: every candidate fragment is kept in a per-pixel list and the
+// lists are replayed in submission order (blends that read the old pixel).
+enum KeyType : uint32_t { KEY_NONE = 0, KEY_MIN = 1, KEY_LAST = 2, KEY_ORDERED = 3 };
 
 // One scene of a batch as the kernels see it.
 struct SceneDev {
@@ -413,7 +416,8 @@ __global__ void __launch_bounds__(kBlock) k_scan(const uint32_t *__restrict__ ro
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == kBlock - 1) {
         totals[0] = base_l + bl;
         totals[1] = base_r + br;
-        totals[2] = 0;
+        totals[2] = 0;  // work counter of k_raster, phase 0
+        totals[3] = 0;  // work counter of k_raster, phase 1 (ordered scenes)
     }
 }
 
@@ -434,7 +438,8 @@ constexpr int kChunkGroup = 16;
 // Rows [y0, y1] of the pixels q0 .. q0+255 of a W-wide scene do not meet the
 // covered rectangle: the whole chunk can be skipped.
 EUC_DEV bool chunk_outside(const uint4 &c, uint64_t q0, uint32_t W) {
-    const uint64_t y0 = q0 / W, y1 = (q0 + kBlock - 1) / W;
+    // pixel indices within a scene fit 32 bits (plan_scene checks W*H)
+    const uint32_t y0 = (uint32_t)q0 / W, y1 = ((uint32_t)q0 + kBlock - 1) / W;
     return y1 < c.y || y0 >= ~c.w;
 }
 
@@ -459,13 +464,17 @@ __global__ void __launch_bounds__(kBlock) k_init(const SceneDev *__restrict__ sc
             const uint64_t pos = c * kBlock;
             si = advance_scene(pix_base, nsc, si, pos);
             const SceneDev &s = sc[si];
-            if (chunk_outside(cov[si], pos - s.pix_base, s.W)) continue;
+            // ordered scenes initialise every entry: their pixel scan sums them all
+            const bool all = s.keytype == KEY_ORDERED;
+            if (!all && chunk_outside(cov[si], pos - s.pix_base, s.W)) continue;
             const uint64_t q = pos + threadIdx.x - s.pix_base;
             if (q >= (uint64_t)s.W * s.H) continue;
-            const uint32_t x = (uint32_t)(q % s.W), y = (uint32_t)(q / s.W);
-            if (!covered(cov[si], x, y)) continue;
+            const uint32_t y = (uint32_t)q / s.W, x = (uint32_t)q - y * s.W;
+            if (!all && !covered(cov[si], x, y)) continue;
             unsigned long long key = ~0ull;
-            if (s.keytype == KEY_MIN) {
+            if (s.keytype == KEY_ORDERED) {
+                key = 0;  // no fragment yet, cursor 0
+            } else if (s.keytype == KEY_MIN) {
                 const float d0 = *reinterpret_cast<const float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x);
                 key = init_key_min(d0, s.depth_test == EUC_TEST_GREATER);
             }
@@ -475,10 +484,10 @@ __global__ void __launch_bounds__(kBlock) k_init(const SceneDev *__restrict__ sc
 }
 
 // ---------------------------------------------------------------------------
-// k_raster: one (primitive, row) per thread; persistent over chunks.
+// k_raster: one (primitive, row) at a time per thread, warp-scheduled.
 // ---------------------------------------------------------------------------
 EUC_DEV void raster_row(const SceneDev &s, const TriRec &r, uint32_t t, uint32_t y,
-                        unsigned long long *__restrict__ vbuf, uint32_t &cnt) {
+                        unsigned long long *__restrict__ vbuf, uint32_t &cnt, int phase, uint2 *__restrict__ frags) {
     // band of this row and the band-clamped bbox (pipeline.rs:341-360, triangles.rs:114-139)
     const uint32_t lo = (y / s.gr) * s.gr;
     const uint32_t hi = min(lo + s.gr, s.H);
@@ -546,6 +555,24 @@ EUC_DEV void raster_row(const SceneDev &s, const TriRec &r, uint32_t t, uint32_t
                 w2 = w2 + d2;
             }
         }
+        if (s.keytype == KEY_ORDERED) {
+            // phase 0 counts each pixel's candidates (low word of its entry);
+            // phase 1 appends (primitive, z) at offset (low word, set by the
+            // pixel scan) + cursor (high word)
+#pragma unroll
+            for (int k = 0; k < kWalk; ++k) {
+                if (!cand[k]) continue;
+                unsigned int *e = reinterpret_cast<unsigned int *>(row_keys + x + k);
+                if (phase == 0) {
+                    ++cnt;
+                    atomicAdd(e, 1u);
+                } else {
+                    const unsigned int slot = __ldcg(e) + atomicAdd(e + 1, 1u);
+                    frags[slot] = make_uint2(t, __float_as_uint(zz[k]));
+                }
+            }
+            continue;
+        }
         unsigned long long key[kWalk];
         bool pass[kWalk];
         float old[kWalk];
@@ -595,7 +622,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_raster(const SceneDev *__restrict
                                                    const uint64_t *__restrict__ live_rowoff,
                                                    unsigned long long *__restrict__ totals,
                                                    const int *__restrict__ err, unsigned long long *__restrict__ vbuf,
-                                                   SceneStats *__restrict__ stats) {
+                                                   SceneStats *__restrict__ stats, int phase,
+                                                   uint2 *__restrict__ frags) {
     __shared__ uint64_t s_off[kBlock / 32][kWarpItems];
     const int lane = threadIdx.x & 31;
     uint64_t *off = s_off[threadIdx.x >> 5];
@@ -606,7 +634,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_raster(const SceneDev *__restrict
     if (gwarp * kWarpItems >= nitems) return;
     for (;;) {
         unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(totals + 2, (unsigned long long)kWarpItems);
+        if (lane == 0) base = atomicAdd(totals + 2 + phase, (unsigned long long)kWarpItems);
         base = __shfl_sync(0xFFFFFFFFu, base, 0);
         if (base >= nitems) break;
         // largest l with live_rowoff[l] <= base; invariant off(lo) <= base < off(hi)
@@ -639,8 +667,9 @@ __global__ void __launch_bounds__(kBlock, 4) k_raster(const SceneDev *__restrict
             const TriRec &r = recs[t];
             const uint32_t scene = r.scene;
             if (err[scene]) continue;
+            if (phase == 1 && sc[scene].keytype != KEY_ORDERED) continue;  // the fill pass is for ordered scenes
             uint32_t cnt = 0;
-            raster_row(sc[scene], r, t, r.by0 + (uint32_t)(i - off[a]), vbuf, cnt);
+            raster_row(sc[scene], r, t, r.by0 + (uint32_t)(i - off[a]), vbuf, cnt, phase, frags);
             if (scene0 == 0xFFFFFFFFu) scene0 = scene;
             if (scene == scene0) cnt0 += cnt;
             else if (cnt) atomicAdd(&stats[scene].candidates, (unsigned long long)cnt);
@@ -715,7 +744,9 @@ __host__ __device__ inline uint64_t quad_row_pairs(uint32_t H, uint32_t gr) {
     return (nb - 1) * ppb + (lh + 1) / 2;
 }
 
-__host__ __device__ inline bool resolve_by_quads(const SceneDev &s) { return s.level == 1 && s.pixel_write; }
+__host__ __device__ inline bool resolve_by_quads(const SceneDev &s) {
+    return s.level == 1 && s.pixel_write && s.keytype != KEY_ORDERED;
+}
 
 // Blocks of k_resolve for one scene.
 __host__ __device__ inline uint64_t resolve_blocks(const SceneDev &s) {
@@ -761,8 +792,8 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
         const uint64_t q = lb * kBlock + tid;
         inside = q < (uint64_t)s.W * s.H;
         if (inside) {
-            x = (uint32_t)(q % s.W);
-            y = (uint32_t)(q / s.W);
+            y = (uint32_t)q / s.W;
+            x = (uint32_t)q - y * s.W;
             lo = (y / s.gr) * s.gr;
         }
     }
@@ -888,6 +919,167 @@ __global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__
             __syncthreads();  // the next chunk reuses shared memory
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Ordered path (KEY_ORDERED): per-pixel fragment lists replayed in order.
+// ---------------------------------------------------------------------------
+constexpr int kOScanPer = 8;
+constexpr int kOScanBlock = kBlock * kOScanPer;
+
+// Sum of the per-pixel candidate counts (low words of vbuf) of each block of
+// kOScanBlock entries in [p0, p1).
+__global__ void __launch_bounds__(kBlock) k_oscan_reduce(const unsigned long long *__restrict__ vbuf, uint64_t p0,
+                                                         uint64_t p1, unsigned long long *__restrict__ bsum) {
+    __shared__ unsigned long long s_a[kBlock / 32 + 1];
+    const uint64_t q0 = p0 + (uint64_t)blockIdx.x * kOScanBlock + (uint64_t)threadIdx.x * kOScanPer;
+    unsigned long long v = 0;
+#pragma unroll
+    for (int k = 0; k < kOScanPer; ++k)
+        if (q0 + k < p1) v += (uint32_t)vbuf[q0 + k];
+    unsigned long long tot;
+    block_excl_scan<unsigned long long>(v, s_a, &tot);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+// Exclusive scan of the counts: the low word of each entry becomes the offset
+// of its pixel's list, the high word (the fill cursor) 0.  total[0] = number
+// of fragments.
+__global__ void __launch_bounds__(kBlock) k_oscan_apply(unsigned long long *__restrict__ vbuf, uint64_t p0, uint64_t p1,
+                                                        const unsigned long long *__restrict__ bsum,
+                                                        unsigned long long *__restrict__ total) {
+    __shared__ unsigned long long s_a[kBlock / 32 + 1];
+    __shared__ unsigned long long s_pre;
+    unsigned long long pre = 0;
+    for (uint64_t j = threadIdx.x; j < blockIdx.x; j += kBlock) pre += bsum[j];
+    unsigned long long tp;
+    block_excl_scan<unsigned long long>(pre, s_a, &tp);
+    if (threadIdx.x == 0) s_pre = tp;
+    __syncthreads();
+    const uint64_t q0 = p0 + (uint64_t)blockIdx.x * kOScanBlock + (uint64_t)threadIdx.x * kOScanPer;
+    uint32_t c[kOScanPer];
+    unsigned long long mine = 0;
+#pragma unroll
+    for (int k = 0; k < kOScanPer; ++k) {
+        c[k] = q0 + k < p1 ? (uint32_t)vbuf[q0 + k] : 0u;
+        mine += c[k];
+    }
+    unsigned long long bt;
+    unsigned long long o = s_pre + block_excl_scan<unsigned long long>(mine, s_a, &bt);
+#pragma unroll
+    for (int k = 0; k < kOScanPer; ++k) {
+        if (q0 + k < p1) vbuf[q0 + k] = (unsigned long long)(uint32_t)o;  // offsets beyond 2^32 are refused by the host
+        o += c[k];
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == kBlock - 1) total[0] = s_pre + bt;
+}
+
+// Fragment of primitive `r` at pixel (x, y): plain or coarse-grid MSAA.
+template <class F>
+EUC_DEV void shade_at(const SceneDev &s, const typename F::U &u, const TriRec &r, const float *__restrict__ vb,
+                      uint32_t x, uint32_t y, float *frag) {
+    const float *v0 = vb + (uint64_t)r.v[0] * F::NV;
+    const float *v1 = vb + (uint64_t)r.v[1] * F::NV;
+    const float *v2 = vb + (uint64_t)r.v[2] * F::NV;
+    float vd[F::NV];
+    if (s.level == 0) {
+        get_v_data<F>(r, v0, v1, v2, (float)x, (float)y, vd);
+        F::fragment(u, vd, frag);
+        return;
+    }
+    const uint32_t L = s.level, lo = (y / s.gr) * s.gr;  // pipeline.rs:541-573
+    const float div = 1.0f / (float)(1u << L);
+    const float fx = rfract((float)x * div), fy = rfract((float)(y - lo) * div);
+    const uint32_t px = x >> L, py = (y - lo) >> L;
+    float t[4][F::NF];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        get_v_data<F>(r, v0, v1, v2, (float)((px + (uint32_t)(c & 1)) << L),
+                      (float)(lo + ((py + (uint32_t)(c >> 1)) << L)), vd);
+        F::fragment(u, vd, t[c]);
+    }
+#pragma unroll
+    for (int i = 0; i < F::NF; ++i) {
+        const float a0 = t[0][i] * (1.0f - fy) + t[2][i] * fy;
+        const float a1 = t[1][i] * (1.0f - fy) + t[3][i] * fy;
+        frag[i] = a0 * (1.0f - fx) + a1 * fx;
+    }
+}
+
+// Replays each pixel's fragments in submission order with euc's sequential
+// depth test (pipeline.rs:519-526) and blend-into-the-current-pixel
+// (pipeline.rs:574-576).  Lists are short in practice; the next fragment is
+// found by a linear scan for the smallest primitive id above the last one.
+template <class F>
+__global__ void __launch_bounds__(kBlock) k_resolve_ordered(const SceneDev *__restrict__ sc,
+                                                            const uint64_t *__restrict__ res_base, int s_begin,
+                                                            int s_end, uint64_t blk_begin,
+                                                            const TriRec *__restrict__ recs,
+                                                            const float *__restrict__ vdata,
+                                                            const unsigned long long *__restrict__ vbuf,
+                                                            const uint2 *__restrict__ frags,
+                                                            const uint4 *__restrict__ cov) {
+    __shared__ int s_scene;
+    const uint64_t blk = blk_begin + blockIdx.x;
+    if (threadIdx.x == 0) s_scene = s_begin + find_scene(res_base + s_begin, s_end - s_begin, blk);
+    __syncthreads();
+    const SceneDev &s = sc[s_scene];
+    const uint64_t q = (blk - res_base[s_scene]) * kBlock + threadIdx.x;
+    if (q >= (uint64_t)s.W * s.H) return;
+    const uint32_t y = (uint32_t)q / s.W, x = (uint32_t)q - y * s.W;
+    if (!covered(cov[s_scene], x, y)) return;
+    const unsigned long long e = vbuf[s.pix_base + q];
+    const uint32_t off = (uint32_t)e, n = (uint32_t)(e >> 32);
+    if (n == 0) return;
+    float *dp = s.depth ? reinterpret_cast<float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x) : nullptr;
+    uint8_t *pp = s.pixel ? s.pixel + (uint64_t)y * s.ppitch + (uint64_t)x * (s.pfmt == EUC_FMT_RGB8 ? 3u : 4u) : nullptr;
+    const bool uses_depth = s.depth_test != EUC_TEST_NONE || s.depth_write;
+    float D = uses_depth ? *dp : 0.0f;
+    const int ri = s.pfmt == EUC_FMT_BGRA8 ? 2 : 0, bi = s.pfmt == EUC_FMT_BGRA8 ? 0 : 2;
+    const int nch = s.pfmt == EUC_FMT_RGB8 ? 3 : 4;
+    uint32_t ch[4] = {0, 0, 0, 255};
+    if (s.pixel_write)
+        for (int i = 0; i < nch; ++i) ch[i] = pp[i];
+    const typename F::U &u = *reinterpret_cast<const typename F::U *>(s.uniforms);
+    const float *vb = vdata + s.vd_base;
+    uint32_t last = 0;  // 1 + the primitive processed last
+    for (uint32_t k = 0; k < n; ++k) {
+        uint32_t best = 0xFFFFFFFFu, bz = 0;
+        for (uint32_t j = 0; j < n; ++j) {
+            const uint2 f = frags[off + j];
+            if (f.x + 1u > last && f.x < best) {
+                best = f.x;
+                bz = f.y;
+            }
+        }
+        last = best + 1u;
+        const float z = __uint_as_float(bz);
+        bool pass = true;
+        if (s.depth_test == EUC_TEST_LESS) pass = z < D;
+        else if (s.depth_test == EUC_TEST_EQUAL) pass = z == D;
+        else if (s.depth_test == EUC_TEST_GREATER) pass = z > D;
+        if (!pass) continue;
+        if (s.depth_write) D = z;
+        if (!s.pixel_write) continue;
+        float frag[F::NF];
+        shade_at<F>(s, u, recs[best], vb, x, y, frag);
+        float c[4] = {frag[0], F::NF > 1 ? frag[F::NF > 1 ? 1 : 0] : 0.0f, F::NF > 2 ? frag[F::NF > 2 ? 2 : 0] : 0.0f,
+                      F::NF > 3 ? frag[F::NF > 3 ? 3 : 0] : 0.0f};
+        if (s.blend == EUC_BLEND_ALPHA) {  // src-over on the unpacked old pixel
+            const float old[4] = {(float)ch[ri] / 255.0f, (float)ch[1] / 255.0f, (float)ch[bi] / 255.0f,
+                                  nch == 3 ? 1.0f : (float)ch[3] / 255.0f};
+            const float a = c[3];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) c[i] = c[i] * a + old[i] * (1.0f - a);
+        }
+        ch[ri] = sat_u8(F::pack(c[0]));
+        ch[1] = sat_u8(F::pack(c[1]));
+        ch[bi] = sat_u8(F::pack(c[2]));
+        if (nch == 4) ch[3] = sat_u8(F::pack(c[3]));
+    }
+    if (s.depth_write) *dp = D;
+    if (s.pixel_write)
+        for (int i = 0; i < nch; ++i) pp[i] = (uint8_t)ch[i];
 }
 
 }  // namespace eucg

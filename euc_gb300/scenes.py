@@ -360,23 +360,25 @@ def soup_triangles(rng, ntris, width, height, area_lo=1.0, area_hi=1e4, extent=1
 
 
 def soup_frame(seed=0, width=1920, height=1080, ntris=200_000, area_lo=1.0, area_hi=1e4,
-               band_rows=abi.BANDS_PAR):
+               band_rows=abi.BANDS_PAR, alpha=False):
     """Clip-space triangle soup: x,y centroids in [-1.2, 1.2] (some cross the
     target edges), z in [0.05, 0.95], w = 1, screen areas log-uniform, per-vertex
     RGBA8 colours, a seeded-permutation u32 index buffer.  RGBA8 + f32 depth,
-    LESS_WRITE, replace blend, no culling (soup orientation is random)."""
+    LESS_WRITE, replace blend, no culling (soup orientation is random).  With
+    `alpha` the colours carry alpha in [32, 255] and the blend is src-over."""
     rng = np.random.default_rng(seed)
     clip = soup_triangles(rng, ntris, width, height, area_lo, area_hi)
     nv = ntris * 3
     col = rng.integers(0, 256, (nv, 4), dtype=np.uint8)
-    col[:, 3] = 255
+    col[:, 3] = rng.integers(32, 256, nv, dtype=np.uint8) if alpha else 255
     perm = rng.permutation(nv).astype(np.uint32)
     vb = np.empty((nv, 20), dtype=np.uint8)
     seq = np.concatenate([clip.astype(np.float32).view(np.uint8).reshape(nv, 16), col], axis=1)
     vb[perm] = seq
     u = abi.VColorUniforms()
     u.mvp = f32mat(np.eye(4))
-    p = PassSpec(make_desc(abi.SHADER_VCOLOR, cull=abi.CULL_NONE, band_rows=band_rows),
+    p = PassSpec(make_desc(abi.SHADER_VCOLOR, cull=abi.CULL_NONE, band_rows=band_rows,
+                           blend=abi.BLEND_ALPHA if alpha else abi.BLEND_REPLACE),
                  layout(20, position=0, color=16), vb.reshape(-1), nv, perm, u, pixel="color", depth="depth")
     return FrameSpec("soup%dx%d_%d" % (width, height, ntris),
                      [TargetSpec("color", width, height, abi.FMT_RGBA8, 0),

@@ -102,6 +102,11 @@ enum euc_wrap {
  * (pipeline.rs:330).  By default such targets use one band (render_seq);
  * this flag reproduces the blank output instead.                             */
 #define EUC_FLAG_PAR_EMPTY 1u
+/* Resolve every candidate fragment in submission order from per-pixel lists
+ * (the path that EUC_BLEND_ALPHA always takes); with a replace blend the
+ * result is the same as the default visibility-key path.  Costs one stream
+ * synchronisation per render (to size the lists).                          */
+#define EUC_FLAG_ORDERED 2u
 
 /* Mirrors the mode methods of `Pipeline` (pipeline.rs:178-209).            */
 typedef struct euc_pipeline_desc {
@@ -290,7 +295,9 @@ int euc_render_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, void *stre
  * device).  Scratch lives in one fixed array inside the library (about 20.8
  * MiB per device that loads it, held until exit).  Limits: 65,536 vertices,
  * 65,536 primitives (index triples), 1,048,576 target pixels; larger scenes
- * return EUC_ERR_CAPACITY.  Runs on the current device, ordered on `stream`.
+ * return EUC_ERR_CAPACITY, and so do order-dependent blends (EUC_BLEND_ALPHA,
+ * EUC_FLAG_ORDERED), whose fragment lists are sized on the device.  Runs on
+ * the current device, ordered on `stream`.
  * `device_status` (nullable, device memory) receives EUC_OK or
  * EUC_ERR_INDEX_OOB once the render has run.  All calls share the scratch
  * array: calls whose work overlaps on the GPU race, so issue them on one

@@ -339,6 +339,14 @@ def _render_band(desc, sh, vout, size, row0, row1, level, pixel, pfmt, depth):
                                         a1 = F(F(t10[i] * F(F(1) - fym)) + F(t11[i] * fym))
                                         frag.append(F(F(a0 * F(F(1) - fxm)) + F(a1 * fxm)))
                                 c = (list(frag) + [F(0)] * 4)[:4]
+                                if desc.blend == abi.BLEND_ALPHA:  # src-over on the unpacked old pixel
+                                    px = [int(v) for v in pixel[y, x, :]]
+                                    if pfmt == abi.FMT_BGRA8:
+                                        px = [px[2], px[1], px[0], px[3]]
+                                    old = [F(F(px[i]) / F(255)) for i in range(3)]
+                                    old.append(F(1) if pfmt == abi.FMT_RGB8 else F(F(px[3]) / F(255)))
+                                    a = c[3]
+                                    c = [F(F(c[i] * a) + F(old[i] * F(F(1) - a))) for i in range(4)]
                                 ch = [as_u8(sh.pack(v)) for v in c]
                                 if pfmt == abi.FMT_BGRA8:
                                     ch = [ch[2], ch[1], ch[0], ch[3]]

@@ -29,8 +29,17 @@ def _mod(make, **desc):
     return wrapped
 
 
-def _soup(seed=1, w=320, h=180, n=4000, hi=3000.0, **desc):
-    return _mod(lambda: scenes.soup_frame(seed=seed, width=w, height=h, ntris=n, area_hi=hi), **desc)
+def _soup(seed=1, w=320, h=180, n=4000, hi=3000.0, alpha=False, **desc):
+    return _mod(lambda: scenes.soup_frame(seed=seed, width=w, height=h, ntris=n, area_hi=hi, alpha=alpha), **desc)
+
+
+def _fmt(make, fmt):
+    def wrapped():
+        f = make()
+        t = f.target("color")
+        f.targets[f.targets.index(t)] = scenes.TargetSpec("color", t.width, t.height, fmt, 0x80402010)
+        return f
+    return wrapped
 
 
 def _clear(make, name, value):
@@ -144,6 +153,21 @@ CASES = {
     "tex_nearest_none": (_textured(abi.FILTER_NEAREST, abi.WRAP_NONE), 0),
     "flat": (_flat(), 0),
     "unindexed": (_unindexed(), 0),
+    # order-dependent blend: per-pixel fragment lists replayed in order
+    "alpha_soup_less": (_soup(seed=21, alpha=True), 0),
+    "alpha_soup_less_pass": (_soup(seed=22, alpha=True, depth_write=0), 0),
+    "alpha_soup_no_depth": (_soup(seed=23, alpha=True, depth_test=abi.TEST_NONE, depth_write=0), 0),
+    "alpha_soup_msaa1": (_soup(seed=24, alpha=True, aa_level=1), 0),
+    "alpha_soup_msaa2_bands": (_soup(seed=25, w=333, h=177, alpha=True, aa_level=2, band_rows=11), 0),
+    "alpha_soup_rgb8": (_fmt(_soup(seed=26, alpha=True), abi.FMT_RGB8), 0),
+    "alpha_soup_bgra8": (_fmt(_soup(seed=27, alpha=True), abi.FMT_BGRA8), 0),
+    # replace blends forced through the ordered path must give the same bytes
+    "ordered_sphere": (_mod(_sphere(seed=3), flags=abi.FLAG_ORDERED), 0),
+    "ordered_soup_less": (_soup(seed=1, flags=abi.FLAG_ORDERED), 0),
+    "ordered_soup_equal": (_clear(_soup(seed=3, depth_test=abi.TEST_EQUAL, flags=abi.FLAG_ORDERED), "depth", 0.5), 0),
+    "ordered_soup_greater": (_clear(_soup(seed=2, depth_test=abi.TEST_GREATER, flags=abi.FLAG_ORDERED), "depth", 0.0), 0),
+    "ordered_knot_aa1": (_mod(_knot(1), flags=abi.FLAG_ORDERED), 1),
+    "ordered_tex_linear_mirror": (_mod(_textured(abi.FILTER_LINEAR, abi.WRAP_MIRROR), flags=abi.FLAG_ORDERED), 0),
 }
 
 

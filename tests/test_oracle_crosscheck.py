@@ -23,9 +23,9 @@ def _run_both(make):
             assert np.array_equal(ref[k], py[k]), k
 
 
-def _soup(seed, w=48, h=32, n=60, hi=400.0, **desc):
+def _soup(seed, w=48, h=32, n=60, hi=400.0, alpha=False, **desc):
     def make():
-        f = scenes.soup_frame(seed=seed, width=w, height=h, ntris=n, area_lo=2.0, area_hi=hi)
+        f = scenes.soup_frame(seed=seed, width=w, height=h, ntris=n, area_lo=2.0, area_hi=hi, alpha=alpha)
         for k, v in desc.items():
             setattr(f.passes[0].desc, k, v)
         return f
@@ -45,6 +45,9 @@ CASES = {
     "soup_depth_only": _soup(6, pixel_write=0),
     "soup_big": _soup(7, w=64, h=48, n=12, hi=6000.0),
     "soup_bands2": _soup(8, band_rows=2),
+    "soup_alpha": _soup(9, alpha=True),
+    "soup_alpha_pass": _soup(10, alpha=True, depth_write=0),
+    "soup_alpha_msaa1": _soup(11, alpha=True, aa_level=1),
     "knot_msaa1": lambda: scenes.knot_frame(seed=1, width=40, height=30, shadow_size=32, tubular=24, radial=6,
                                             tex_size=16, aa_level=1),
     "knot_msaa2_bands": lambda: scenes.knot_frame(seed=2, width=44, height=30, shadow_size=32, tubular=24, radial=6,
