@@ -51,6 +51,10 @@ WORKLOADS = {
              "per-vertex RGBA8, LESS_WRITE, permuted u32 indices", 1, "frames/s"),
     "knot": ("two passes: 2048^2 f32 shadow map, then 1920x1080 RGBA8 textured Phong (1024^2 value noise, "
              "tiled bilinear) with Msaa{level:1}; (2,3) torus knot, 500k tris", 4, "frames/s"),
+    "serve": ("serving loop: Poisson arrivals, 64 resident meshes (tris logU[100,1e5], sphere/knot/soup) and 32 "
+              "resident 512^2 RGBA8 textures, two passes (res^2 f32 shadow map, textured Phong + shadow into "
+              "RGBA8 + f32 depth), res U{64,128,256,512}^2, 50% Msaa{level:1}, colour read back to pinned host "
+              "memory, 40 GB framebuffer budget", 512, "requests/s"),
 }
 WORKLOAD = WORKLOADS["batch"][0]
 
@@ -71,6 +75,10 @@ def parse():
                     help="batch: the 256 uneven scenes (default); sphere / soup / knot: the small plain, "
                          "fill-rate and two-pass configurations, --frames of them per step")
     ap.add_argument("--frames", type=int, default=0, help="frames per step for sphere/soup/knot (0 = default)")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape (no autotuning)")
+    ap.add_argument("--no-graph", action="store_true", help="time plain euc_render_batch calls only")
+    ap.add_argument("--rates", default="2000,10000,50000", help="serve: Poisson arrival rates (requests/s)")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="serve: length of each rate's run")
     args = ap.parse_args()
     if args.workload != "batch":
         args.scenes = args.frames or WORKLOADS[args.workload][1]
@@ -93,6 +101,10 @@ def make_frames(args, rank):
         return [scenes.soup_frame(seed=seed + i) for i in range(args.scenes)]
     if args.workload == "knot":
         return [scenes.knot_frame(seed=seed + i) for i in range(args.scenes)]
+    if args.workload == "serve":
+        assets = scenes.serve_assets(seed=seed)
+        rng = np.random.default_rng(seed + 1)
+        return [scenes.serve_frame(assets, rng) for _ in range(args.scenes)]
     return scenes.batch_frames(seed=seed, n=args.scenes)
 
 
@@ -282,8 +294,20 @@ def run_gpu(args):
     def step():
         fr.render_batch(ctx, batch, stream, clear=True)
 
+    tuning, tune_info = None, None
+    if not args.no_tune:
+        from euc_gb300 import autotune
+        tuning, tune_info = autotune.tune(ctx, batch, stream)
+    # the recorded form of the same batch (scenes on the ordered path cannot be recorded)
+    graph = None
+    if not args.no_graph and not any(s.desc.blend == 1 or s.desc.flags & 2 for arr in batch.scene_arrays()
+                                     for s in arr):
+        graph = fr.BatchGraph(ctx, batch)
+
     for _ in range(max(args.warmup, 3)):
         step()
+        if graph:
+            graph.launch(stream)
     capi.check(ctx.sync(fr._stream_ptr(stream)), "warm-up")
     # candidate fragments of one step, pass by pass (stats cover one batch call)
     cand_per_step = 0
@@ -312,21 +336,38 @@ def run_gpu(args):
     torch.cuda.synchronize()
     clocks.start()
     time.sleep(0.3)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
+
+    def timed(fn):
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1)
+        if world > 1:
+            tt = torch.tensor([t], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            dist.barrier()
+            t = float(tt.item())
+        return t
+
+    # plain calls with per-stage CUDA events (the stage times of the roofline)
+    ms_plain = timed(step)
     ctx.set_profiling(False)
     stage_ms, launches = ctx.profile()
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.barrier()
-        ms = float(t.item())
+    ms_graph = None
+    if graph:
+        ms_graph = timed(lambda: graph.launch(stream))
+        _, graph_launches = ctx.profile()
+    clk = clocks.stop()
+    ms = min(ms_plain, ms_graph) if ms_graph else ms_plain
+    form = "graph" if ms_graph and ms_graph <= ms_plain else "plain"
+    if form == "graph":
+        launches = graph_launches
     ms_step = ms / args.steps
     value = world * args.scenes / (ms_step / 1e3)
 
@@ -372,6 +413,10 @@ def run_gpu(args):
                        "l2": "no flush: %.0f MB of inputs and targets per step > 129 MB L2" % (
                            (alg_bytes + 8 * sum(t.width * t.height for f in specs for t in f.targets if t.fmt != 4)) / 1e6),
                        "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "form": {"timed": "euc_graph replay" if form == "graph" else "euc_render_batch calls",
+                     "plain_value": world * args.scenes / (ms_plain / args.steps / 1e3),
+                     "graph_value": world * args.scenes / (ms_graph / args.steps / 1e3) if ms_graph else None,
+                     "tuning": tuning.as_dict() if tuning is not None else None, "autotune": tune_info},
             "per_scene": {"value": per_scene, "unit": unit, "path": "euc_render per scene"},
             "batched_speedup": value / world / per_scene if per_scene else None,
             "mfrag_per_s": cand_per_step * world / (ms_step / 1e3) / 1e6,
@@ -388,15 +433,96 @@ def run_gpu(args):
             "clocks": clk,
         }
         print(json.dumps(out), flush=True)
+    if graph:
+        graph.close()
     ctx.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+def run_serve(args):
+    """The serving loop under open-loop Poisson arrivals, one run per rate.
+    Requests draw uniformly from a pool of `--scenes` seeded two-pass
+    requests over the resident meshes and textures; each run reports
+    latency percentiles (arrival to colour on the host) and throughput."""
+    import ctypes as C
+
+    import torch
+    import torch.distributed as dist
+    from euc_gb300 import abi, serve
+
+    world, rank, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    frames = make_frames(args, rank)
+    srv = serve.Server(local, framebuffer_budget=40 << 30, max_batch=256, slots=3)
+    res = serve.Resident(srv)
+    pins, keep, pool, outs = [], [], [], []
+    for k, f in enumerate(frames):
+        n = serve.out_bytes(f, ("color",))
+        bufs = [torch.empty(n, dtype=torch.uint8).pin_memory() for _ in range(4)]
+        pins += bufs
+        outs.append([(b.data_ptr(), n) for b in bufs])
+        r, kp = serve.request_for(f, res, ("color",), tag=k, out=bufs[0].data_ptr(), out_size=n)
+        pool.append(r)
+        keep.append(kp)
+    arr = (abi.ServerRequest * len(pool))(*pool)
+    for _ in range(max(args.warmup, 3)):  # sizes every slot's scratch
+        srv.submit(arr)
+        srv.drain()
+        while len(srv.poll(8192)):
+            pass
+    base = srv.stats()
+    bus = None
+    try:
+        bus = torch.cuda.get_device_properties(local).pci_bus_id
+    except AttributeError:
+        pass
+    runs = []
+    clocks = ClockSampler(bus)
+    clocks.start()
+    for i, rate in enumerate(float(r) for r in args.rates.split(",")):
+        _, summ = serve.run_poisson(srv, arr, outs, rate, args.serve_seconds, seed=args.seed + 17 * i + rank)
+        summ.pop("stats")
+        runs.append(summ)
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    top = runs[-1]
+    tot = [torch.tensor([r["throughput"]], device="cuda:%d" % local) for r in runs]
+    if world > 1:
+        for t in tot:
+            dist.all_reduce(t)
+        dist.destroy_process_group()
+    if rank == 0:
+        desc, _, unit = WORKLOADS["serve"]
+        per_req_out = float(np.mean([serve.out_bytes(f, ("color",)) for f in frames]))
+        out = {
+            "metric": "served requests/s with p50/p99 latency (arrival to colour on host)", "value": float(tot[-1].item()),
+            "unit": unit, "n_gpus": world, "steps": len(runs), "warmup": max(args.warmup, 3),
+            "ms_per_step": 1e3 * args.serve_seconds, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators), meshes/textures resident",
+            "config": {"workload": desc, "name": "serve", "pool": len(frames), "seed": args.seed,
+                       "rates": args.rates, "seconds_per_rate": args.serve_seconds, "max_batch": 256, "slots": 3,
+                       "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
+            "serving": runs,
+            "gpu_launches": int(st["launches"] - base["launches"]),
+            "e2e": {"value": float(tot[-1].item()), "unit": unit, "h2d_bytes_per_step": None,
+                    "d2h_bytes_per_step": per_req_out * top["completed"],
+                    "path": "euc_server_submit -> completion with colour in pinned host memory"},
+            "roofline": None, "cpu_baseline": None, "clocks": clk,
+        }
+        print(json.dumps(out), flush=True)
 
 
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_gpu(args)
 

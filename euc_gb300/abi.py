@@ -18,12 +18,16 @@ ERR_BAND = 6
 ERR_TIMEOUT = 7
 ERR_BUDGET = 8
 ERR_CAPACITY = 9
+ERR_STALE = 10
+ERR_BUSY = 11
 
 STATUS_NAMES = {
     OK: "EUC_OK", ERR_INVALID: "EUC_ERR_INVALID", ERR_SIZE_MISMATCH: "EUC_ERR_SIZE_MISMATCH",
     ERR_INDEX_OOB: "EUC_ERR_INDEX_OOB", ERR_OOM: "EUC_ERR_OOM", ERR_CUDA: "EUC_ERR_CUDA",
     ERR_BAND: "EUC_ERR_BAND", ERR_TIMEOUT: "EUC_ERR_TIMEOUT", ERR_BUDGET: "EUC_ERR_BUDGET",
     ERR_CAPACITY: "EUC_ERR_CAPACITY",
+    ERR_STALE: "EUC_ERR_STALE",
+    ERR_BUSY: "EUC_ERR_BUSY",
 }
 
 TEST_NONE, TEST_LESS, TEST_EQUAL, TEST_GREATER = 0, 1, 2, 3
@@ -113,6 +117,14 @@ class Stats(C.Structure):
     _fields_ = [("triangles", C.c_uint64), ("culled", C.c_uint64), ("candidates", C.c_uint64)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("raster_blocks_per_sm", C.c_uint32), ("raster_warp_rows", C.c_uint32),
+                ("chunk_group", C.c_uint32), ("chunk_blocks_per_sm", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
 class Scene(C.Structure):
     _fields_ = [("desc", PipelineDesc), ("layout", VertexLayout), ("vertices", C.c_void_p),
                 ("nverts", C.c_uint64), ("indices", C.c_void_p), ("nindices", C.c_uint64),
@@ -128,3 +140,48 @@ def mat4(values):
 
 def status_name(code):
     return STATUS_NAMES.get(code, "EUC_STATUS_%d" % code)
+
+
+# ---- serving --------------------------------------------------------------
+SERVER_MAX_TARGETS = 4
+SERVER_MAX_PASSES = 4
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_batch", C.c_uint32), ("framebuffer_budget", C.c_uint64),
+                ("slots", C.c_uint32), ("max_pending", C.c_uint32)]
+
+
+class ServerTarget(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("format", C.c_uint32), ("clear", C.c_uint32),
+                ("readback", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class ServerBinding(C.Structure):
+    _fields_ = [("offset", C.c_uint32), ("texture", C.c_int32), ("target", C.c_int32), ("reserved", C.c_uint32)]
+
+
+class ServerPass(C.Structure):
+    _fields_ = [("desc", PipelineDesc), ("mesh", C.c_uint32), ("pixel_target", C.c_int32),
+                ("depth_target", C.c_int32), ("nbindings", C.c_uint32), ("bindings", C.POINTER(ServerBinding)),
+                ("uniforms", C.c_void_p), ("uniforms_size", C.c_uint64)]
+
+
+class ServerRequest(C.Structure):
+    _fields_ = [("tag", C.c_uint64), ("arrival_ns", C.c_uint64), ("out", C.c_void_p), ("out_size", C.c_uint64),
+                ("ntargets", C.c_uint32), ("npasses", C.c_uint32), ("targets", C.POINTER(ServerTarget)),
+                ("passes", C.POINTER(ServerPass))]
+
+
+class ServerCompletion(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("tag", C.c_uint64), ("status", C.c_int32), ("batch_size", C.c_uint32),
+                ("arrival_ns", C.c_uint64), ("admit_ns", C.c_uint64), ("done_ns", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("submitted", "completed", "failed", "refused", "pending", "in_flight",
+                                          "batches", "batched_requests", "budget_bytes", "budget_used",
+                                          "budget_peak", "launches")]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libeuc_gb300.so")
-SOURCES = [os.path.join(HERE, "csrc", "euc_capi.cu")]
+SOURCES = [os.path.join(HERE, "csrc", f) for f in ("euc_capi.cu", "euc_server.cu")]
 HEADERS = [os.path.join(HERE, "csrc", f) for f in ("euc_device.cuh", "euc_kernels.cuh")] + [
     os.path.join(ROOT, "include", "euc_gb300.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -35,10 +35,27 @@ def build(force=False, verbose=False, extra=()):
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [nvcc()] + ARCH + NVCC_FLAGS + list(extra) + SOURCES + ["-o", tmp]
-    if verbose:
-        print(" ".join(cmd), flush=True)
-    subprocess.run(cmd, check=True)
+    compile_flags = [f for f in NVCC_FLAGS if f != "-shared"]
+    objs, procs = [], []
+    for src in SOURCES:  # translation units compile in parallel
+        obj = os.path.join(OUT_DIR, os.path.basename(src) + ".%d.o" % os.getpid())
+        cmd = [nvcc()] + ARCH + compile_flags + list(extra) + ["-c", src, "-o", obj]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        procs.append(subprocess.Popen(cmd))
+        objs.append(obj)
+    failed = [p.args for p in procs if p.wait() != 0]
+    try:
+        if failed:
+            raise subprocess.CalledProcessError(1, failed[0])
+        cmd = [nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fPIC"] + objs + ["-o", tmp]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        subprocess.run(cmd, check=True)
+    finally:
+        for o in objs:
+            if os.path.exists(o):
+                os.remove(o)
     os.replace(tmp, LIB)
     return LIB
 

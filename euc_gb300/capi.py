@@ -27,8 +27,26 @@ SIGNATURES = {
                                   C.POINTER(abi.VertexLayout), C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
                                   C.POINTER(abi.Target), C.POINTER(abi.Target)]),
     "euc_render_batch": (C.c_int, [C.c_void_p, C.POINTER(abi.Scene), C.c_size_t, C.c_void_p]),
+    "euc_graph_create": (C.c_int, [C.c_void_p, C.POINTER(abi.Scene), C.c_size_t, C.POINTER(C.c_void_p)]),
+    "euc_graph_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "euc_graph_destroy": (C.c_int, [C.c_void_p]),
+    "euc_ctx_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(abi.Tuning)]),
+    "euc_ctx_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(abi.Tuning)]),
     "euc_ctx_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "euc_ctx_profile": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
+    "euc_server_create": (C.c_int, [C.POINTER(abi.ServerConfig), C.POINTER(C.c_void_p)]),
+    "euc_server_destroy": (C.c_int, [C.c_void_p]),
+    "euc_server_add_mesh": (C.c_int, [C.c_void_p, C.POINTER(abi.VertexLayout), C.c_void_p, C.c_size_t, C.c_void_p,
+                                      C.c_size_t, C.POINTER(C.c_uint32)]),
+    "euc_server_add_texture": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32,
+                                         C.POINTER(C.c_uint32)]),
+    "euc_server_now_ns": (C.c_uint64, [C.c_void_p]),
+    "euc_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_uint64),
+                                    C.POINTER(C.c_size_t)]),
+    "euc_server_poll": (C.c_int, [C.c_void_p, C.POINTER(abi.ServerCompletion), C.c_size_t, C.POINTER(C.c_size_t),
+                                  C.c_int]),
+    "euc_server_drain": (C.c_int, [C.c_void_p, C.c_int]),
+    "euc_server_stats_get": (C.c_int, [C.c_void_p, C.POINTER(abi.ServerStats)]),
     "euc_render_noalloc": (C.c_int, [C.POINTER(abi.PipelineDesc), C.c_void_p, C.c_size_t, C.POINTER(abi.VertexLayout),
                                      C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(abi.Target),
                                      C.POINTER(abi.Target), C.c_void_p, C.c_void_p]),
@@ -107,6 +125,17 @@ class Context:
         check(lib().euc_ctx_stats(self.handle, stream, C.byref(s)), "euc_ctx_stats")
         return s
 
+    def set_tuning(self, tuning=None, **kw):
+        """Sets the launch shape (abi.Tuning or its fields as keywords; None or
+        no fields restores the defaults)."""
+        t = tuning if tuning is not None else abi.Tuning(**kw)
+        check(lib().euc_ctx_set_tuning(self.handle, C.byref(t)), "euc_ctx_set_tuning")
+
+    def get_tuning(self):
+        t = abi.Tuning()
+        check(lib().euc_ctx_get_tuning(self.handle, C.byref(t)), "euc_ctx_get_tuning")
+        return t
+
     def set_profiling(self, on):
         check(lib().euc_ctx_set_profiling(self.handle, 1 if on else 0), "euc_ctx_set_profiling")
 
@@ -137,3 +166,31 @@ class Context:
     def render_scene_array(self, arr, stream=None):
         """euc_render_batch on a prebuilt ctypes array of abi.Scene."""
         return lib().euc_render_batch(self.handle, arr, len(arr), stream)
+
+    def graph(self, arr):
+        """Records a batch (ctypes array of abi.Scene) as a replayable Graph."""
+        return Graph(self, arr)
+
+
+class Graph:
+    """euc_graph: a batch recorded once, replayed with one launch."""
+
+    def __init__(self, ctx, arr):
+        self.ctx = ctx
+        h = C.c_void_p()
+        check(lib().euc_graph_create(ctx.handle, arr, len(arr), C.byref(h)), "euc_graph_create")
+        self.handle = h
+
+    def launch(self, stream=None):
+        check(lib().euc_graph_launch(self.handle, stream), "euc_graph_launch")
+
+    def close(self):
+        if self.handle:
+            lib().euc_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -43,7 +43,9 @@ struct euc_ctx {
     int nsm = 0;
     DevBuf clip, vdata, recs, rows, chunk_sums, live_tri, live_rowoff, totals, vbuf, err, stats, cov;
     DevBuf obsum, frags;  // ordered path: pixel-scan block sums, fragment lists
+    DevBuf plan;          // k_plan: k_init and k_resolve chunk bases (2 x (scenes + 1))
     int raster_blocks = 0;  // resident k_raster blocks per SM
+    euc_tuning tune{};      // launch-shape overrides (0 = default)
     // buffers used by euc_render_host
     DevBuf h_verts, h_idx, h_pixel, h_depth, h_tex[2];
     StageSlot slots[kStageSlots];
@@ -51,6 +53,7 @@ struct euc_ctx {
     int last_nscenes = 0;
     // profiling: event pairs per stage, pooled
     bool profiling = false;
+    bool capturing = false;  // a graph is being recorded: no profiling events
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_marks;
@@ -262,6 +265,18 @@ int plan_scene(const euc_scene &sc, Plan &p) {
     return EUC_OK;
 }
 
+}  // namespace
+
+namespace eucg {
+// The scene checks of the render path, for the serving loop's submissions.
+__attribute__((visibility("hidden"))) int check_scene(const euc_scene *s) {
+    Plan p;
+    return s ? plan_scene(*s, p) : EUC_ERR_INVALID;
+}
+}  // namespace eucg
+
+namespace {
+
 int acquire_slot(euc_ctx *ctx, size_t bytes, StageSlot *&out) {
     StageSlot &s = ctx->slots[ctx->next_slot];
     ctx->next_slot = (ctx->next_slot + 1) % kStageSlots;
@@ -287,17 +302,19 @@ int acquire_slot(euc_ctx *ctx, size_t bytes, StageSlot *&out) {
 // Chunks per group of the chunk-group kernels (k_init, k_resolve): 1 while
 // the launch has fewer chunks than 16 blocks per SM can hold, growing to
 // kChunkGroup for large batches so that the scene search is amortised.
-uint32_t chunk_group(uint64_t nchunks, int nsm) {
-    const uint64_t slots = (uint64_t)(nsm > 0 ? nsm : 1) * 16;
+// `group` > 0 and `per_sm` > 0 override the size and the per-SM cap.
+uint32_t chunk_group(uint64_t nchunks, int nsm, uint32_t group = 0, uint32_t per_sm = 0) {
+    if (group) return group;
+    const uint64_t slots = (uint64_t)(nsm > 0 ? nsm : 1) * (per_sm ? per_sm : 16);
     return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(kChunkGroup, nchunks / slots));
 }
 
 // Grid of the chunk-group kernels: one block per group, at most 16 blocks per
 // SM (the blocks stride the groups).
-unsigned chunk_grid(uint64_t nchunks, int nsm) {
-    const uint32_t g = chunk_group(nchunks, nsm);
+unsigned chunk_grid(uint64_t nchunks, int nsm, uint32_t group = 0, uint32_t per_sm = 0) {
+    const uint32_t g = chunk_group(nchunks, nsm, group, per_sm);
     const uint64_t groups = (nchunks + g - 1) / g;
-    const uint64_t cap = (uint64_t)(nsm > 0 ? nsm : 1) * 16;
+    const uint64_t cap = (uint64_t)(nsm > 0 ? nsm : 1) * (per_sm ? per_sm : 16);
     return (unsigned)std::max<uint64_t>(1, std::min(groups, cap));
 }
 
@@ -317,7 +334,7 @@ int raster_blocks_per_sm() {
 
 // Records an event on `st` when profiling; returns nullptr otherwise.
 cudaEvent_t prof_event(euc_ctx *ctx, cudaStream_t st) {
-    if (!ctx->profiling) return nullptr;
+    if (!ctx->profiling || ctx->capturing) return nullptr;
     if (ctx->ev_used == ctx->ev_pool.size()) {
         cudaEvent_t e;
         if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
@@ -338,15 +355,17 @@ void launch_vertex(const SceneDev *sc, const uint64_t *vb, int s0, int s1, uint6
     if (nblk) k_vertex<F><<<(unsigned)nblk, kBlock, 0, st>>>(sc, vb, s0, s1, blk0, (float4 *)ctx->clip.p, (float *)ctx->vdata.p);
 }
 
+// rbase: the device chunk bases of k_plan; nblk: an upper bound of the
+// chunks of scenes [s0, s1) (their whole targets), which sizes the grid.
 template <class F>
-void launch_resolve(const SceneDev *sc, const uint64_t *pb, int s0, int s1, uint64_t blk0, uint64_t nblk, euc_ctx *ctx,
+void launch_resolve(const SceneDev *sc, const uint64_t *rbase, int s0, int s1, uint64_t nblk, euc_ctx *ctx,
                     cudaStream_t st) {
-    if (nblk)
-        k_resolve<F><<<chunk_grid(nblk, ctx->nsm), kBlock, 0, st>>>(sc, pb, s0, s1, blk0, nblk,
-                                                                    chunk_group(nblk, ctx->nsm),
-                                                                    (const TriRec *)ctx->recs.p, (const float *)ctx->vdata.p,
-                                                                    (const unsigned long long *)ctx->vbuf.p,
-                                                                    (const uint4 *)ctx->cov.p);
+    if (!nblk) return;
+    const euc_tuning &tu = ctx->tune;
+    k_resolve<F><<<chunk_grid(nblk, ctx->nsm, tu.chunk_group, tu.chunk_blocks_per_sm), kBlock, 0, st>>>(
+        sc, rbase, s0, s1, chunk_group(nblk, ctx->nsm, tu.chunk_group, tu.chunk_blocks_per_sm),
+        (const TriRec *)ctx->recs.p, (const float *)ctx->vdata.p, (const unsigned long long *)ctx->vbuf.p,
+        (const uint4 *)ctx->cov.p);
 }
 
 void dispatch_vertex(uint32_t shader, const SceneDev *sc, const uint64_t *vb, int s0, int s1, uint64_t blk0, uint64_t nblk,
@@ -361,15 +380,15 @@ void dispatch_vertex(uint32_t shader, const SceneDev *sc, const uint64_t *vb, in
     }
 }
 
-void dispatch_resolve(uint32_t shader, const SceneDev *sc, const uint64_t *pb, int s0, int s1, uint64_t blk0,
-                      uint64_t nblk, euc_ctx *ctx, cudaStream_t st) {
+void dispatch_resolve(uint32_t shader, const SceneDev *sc, const uint64_t *rbase, int s0, int s1, uint64_t nblk,
+                      euc_ctx *ctx, cudaStream_t st) {
     switch (shader) {
-    case EUC_SHADER_FLAT: launch_resolve<FlatFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
-    case EUC_SHADER_VCOLOR: launch_resolve<VColorFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
-    case EUC_SHADER_GOURAUD: launch_resolve<GouraudFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
-    case EUC_SHADER_TEXTURED: launch_resolve<TexturedFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
-    case EUC_SHADER_PHONG: launch_resolve<PhongFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
-    case EUC_SHADER_SHADOW: launch_resolve<ShadowFn>(sc, pb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_FLAT: launch_resolve<FlatFn>(sc, rbase, s0, s1, nblk, ctx, st); break;
+    case EUC_SHADER_VCOLOR: launch_resolve<VColorFn>(sc, rbase, s0, s1, nblk, ctx, st); break;
+    case EUC_SHADER_GOURAUD: launch_resolve<GouraudFn>(sc, rbase, s0, s1, nblk, ctx, st); break;
+    case EUC_SHADER_TEXTURED: launch_resolve<TexturedFn>(sc, rbase, s0, s1, nblk, ctx, st); break;
+    case EUC_SHADER_PHONG: launch_resolve<PhongFn>(sc, rbase, s0, s1, nblk, ctx, st); break;
+    case EUC_SHADER_SHADOW: launch_resolve<ShadowFn>(sc, rbase, s0, s1, nblk, ctx, st); break;
     }
 }
 
@@ -396,7 +415,19 @@ void dispatch_resolve_ordered(uint32_t shader, const SceneDev *sc, const uint64_
 }
 
 // Runs a batch of scenes.  All pointers inside `scenes` are device pointers.
-int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) {
+// Staging supplied by a CUDA graph instead of the context's ring.  With
+// `dry` the batch is planned and the scratch buffers are sized, nothing is
+// enqueued, and `need` returns the staging bytes.  Otherwise `host` / `dev`
+// (at least `need` bytes, owned by the graph) carry the scene tables, no
+// stream is synchronised and the ordered path (which synchronises) is refused.
+struct StageOverride {
+    bool dry = false;
+    void *host = nullptr;
+    void *dev = nullptr;
+    size_t need = 0;
+};
+
+int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, StageOverride *so = nullptr) {
     std::vector<Plan> plans;
     plans.reserve(n);
     for (size_t i = 0; i < n; ++i) {
@@ -445,38 +476,44 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
     if ((rc = grow(ctx->err, ns * sizeof(int)))) return rc;
     if ((rc = grow(ctx->stats, ns * sizeof(SceneStats)))) return rc;
     if ((rc = grow(ctx->cov, ns * sizeof(uint4)))) return rc;
-    // staging: scene table | vtx bases | tri bases | pix bases | uniforms
+    if ((rc = grow(ctx->plan, 2 * (ns + 1) * sizeof(uint64_t)))) return rc;
+    // staging: scene table | vtx bases | tri bases | resolve bases | uniforms
     const size_t off_sc = 0;
     const size_t off_vb = pad_up(ns * sizeof(SceneDev), 16);
     const size_t off_tb = off_vb + pad_up(ns * sizeof(uint64_t), 16);
-    const size_t off_pb = off_tb + pad_up(ns * sizeof(uint64_t), 16);
-    const size_t off_rb = off_pb + pad_up(ns * sizeof(uint64_t), 16);
+    const size_t off_rb = off_tb + pad_up(ns * sizeof(uint64_t), 16);
     size_t off_u = off_rb + pad_up(ns * sizeof(uint64_t), 16);
     std::vector<size_t> uoff(ns);
     for (int i = 0; i < ns; ++i) {
         uoff[i] = off_u;
         off_u += pad_up(plans[i].usize, 16);
     }
+    if (so) {
+        if (plans.back().d.keytype == KEY_ORDERED) return EUC_ERR_INVALID;  // a graph cannot synchronise
+        if (so->dry) {
+            so->need = off_u;
+            return EUC_OK;
+        }
+        if (off_u > so->need) return EUC_ERR_INVALID;
+    }
     StageSlot *slot = nullptr;
-    if ((rc = acquire_slot(ctx, off_u, slot))) return rc;
-    uint8_t *h = (uint8_t *)slot->host;
-    uint8_t *dv = (uint8_t *)slot->dev;
+    if (!so && (rc = acquire_slot(ctx, off_u, slot))) return rc;
+    uint8_t *h = (uint8_t *)(so ? so->host : slot->host);
+    uint8_t *dv = (uint8_t *)(so ? so->dev : slot->dev);
     SceneDev *hsc = (SceneDev *)(h + off_sc);
-    uint64_t *hvb = (uint64_t *)(h + off_vb), *htb = (uint64_t *)(h + off_tb), *hpb = (uint64_t *)(h + off_pb),
-             *hrb = (uint64_t *)(h + off_rb);
+    uint64_t *hvb = (uint64_t *)(h + off_vb), *htb = (uint64_t *)(h + off_tb), *hrb = (uint64_t *)(h + off_rb);
     for (int i = 0; i < ns; ++i) {
         std::memcpy(h + uoff[i], plans[i].uniforms, plans[i].usize);
         plans[i].d.uniforms = dv + uoff[i];
         hsc[i] = plans[i].d;
         hvb[i] = plans[i].d.vtx_base;
         htb[i] = plans[i].d.tri_base;
-        hpb[i] = plans[i].d.pix_base;
         hrb[i] = res_base[i];
     }
-    CUDA_TRY(cudaMemcpyAsync(slot->dev, slot->host, off_u, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(dv, h, off_u, cudaMemcpyHostToDevice, st));
     const SceneDev *dsc = (const SceneDev *)(dv + off_sc);
     const uint64_t *dvb = (const uint64_t *)(dv + off_vb), *dtb = (const uint64_t *)(dv + off_tb),
-                   *dpb = (const uint64_t *)(dv + off_pb), *drb = (const uint64_t *)(dv + off_rb);
+                   *drb = (const uint64_t *)(dv + off_rb);
     CUDA_TRY(cudaMemsetAsync(ctx->err.p, 0, ns * sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(ctx->stats.p, 0, ns * sizeof(SceneStats), st));
     CUDA_TRY(cudaMemsetAsync(ctx->cov.p, 0xFF, ns * sizeof(uint4), st));  // empty rectangles
@@ -499,17 +536,23 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
     k_scan<<<(unsigned)nscan, kBlock, 0, st>>>((const uint32_t *)ctx->rows.p, (const uint2 *)ctx->chunk_sums.p, tri,
                                                (uint32_t *)ctx->live_tri.p, (uint64_t *)ctx->live_rowoff.p,
                                                (unsigned long long *)ctx->totals.p);
+    uint64_t *const ibase = (uint64_t *)ctx->plan.p, *const rbase = ibase + ns + 1;
+    k_plan<<<1, kBlock, 0, st>>>(dsc, ns, (const uint4 *)ctx->cov.p, ibase, rbase);
     cudaEvent_t e3 = prof_event(ctx, st);
-    k_init<<<chunk_grid(pix / kBlock, ctx->nsm), kBlock, 0, st>>>(dsc, dpb, ns, (const uint4 *)ctx->cov.p,
-                                                                   (unsigned long long *)ctx->vbuf.p, pix / kBlock,
-                                                                   chunk_group(pix / kBlock, ctx->nsm));
+    const euc_tuning &tu = ctx->tune;
+    const uint64_t ichunks = (pix + kInitChunk - 1) / kInitChunk + ns;  // bounds the chunks k_plan counts
+    k_init<<<chunk_grid(ichunks, ctx->nsm, tu.chunk_group, tu.chunk_blocks_per_sm), kBlock, 0, st>>>(
+        dsc, ibase, ns, (const uint4 *)ctx->cov.p, (unsigned long long *)ctx->vbuf.p,
+        chunk_group(ichunks, ctx->nsm, tu.chunk_group, tu.chunk_blocks_per_sm));
     cudaEvent_t e4 = prof_event(ctx, st);
-    const unsigned rgrid = (unsigned)(ctx->nsm * ctx->raster_blocks);
+    const unsigned rgrid = (unsigned)(ctx->nsm * (tu.raster_blocks_per_sm ? (int)tu.raster_blocks_per_sm
+                                                                           : ctx->raster_blocks));
+    const int witems = tu.raster_warp_rows ? (int)tu.raster_warp_rows : kWarpItems;
     k_raster<<<rgrid, kBlock, 0, st>>>(dsc, (const TriRec *)ctx->recs.p, (const uint32_t *)ctx->live_tri.p,
                                        (const uint64_t *)ctx->live_rowoff.p, (unsigned long long *)ctx->totals.p,
                                        (const int *)ctx->err.p, (unsigned long long *)ctx->vbuf.p,
-                                       (SceneStats *)ctx->stats.p, 0, nullptr);
-    ctx->launches += 4;
+                                       (SceneStats *)ctx->stats.p, 0, nullptr, witems);
+    ctx->launches += 5;
     // ordered scenes: scan the per-pixel counts, size the fragment buffer
     // (one stream synchronisation), fill the lists in a second raster pass
     int first_ordered = ns;
@@ -531,7 +574,7 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
         k_raster<<<rgrid, kBlock, 0, st>>>(dsc, (const TriRec *)ctx->recs.p, (const uint32_t *)ctx->live_tri.p,
                                            (const uint64_t *)ctx->live_rowoff.p, (unsigned long long *)ctx->totals.p,
                                            (const int *)ctx->err.p, (unsigned long long *)ctx->vbuf.p,
-                                           (SceneStats *)ctx->stats.p, 1, (uint2 *)ctx->frags.p);
+                                           (SceneStats *)ctx->stats.p, 1, (uint2 *)ctx->frags.p, witems);
         ctx->launches += 3;
     }
     cudaEvent_t e5 = prof_event(ctx, st);
@@ -543,7 +586,7 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
         if (plans[a].d.keytype == KEY_ORDERED)
             dispatch_resolve_ordered(plans[a].d.shader, dsc, drb, a, b, blk0, blk1 - blk0, ctx, st);
         else
-            dispatch_resolve(plans[a].d.shader, dsc, drb, a, b, blk0, blk1 - blk0, ctx, st);
+            dispatch_resolve(plans[a].d.shader, dsc, rbase, a, b, blk1 - blk0, ctx, st);
         ctx->launches += blk1 > blk0;
         a = b;
     }
@@ -555,8 +598,10 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st) 
     prof_mark(ctx, EUC_STAGE_RASTER, e4, e5);
     prof_mark(ctx, EUC_STAGE_RESOLVE, e5, e6);
     CUDA_TRY(cudaGetLastError());
-    CUDA_TRY(cudaEventRecord(slot->done, st));
-    slot->pending = true;
+    if (slot) {
+        CUDA_TRY(cudaEventRecord(slot->done, st));
+        slot->pending = true;
+    }
     return EUC_OK;
 }
 
@@ -578,6 +623,7 @@ const char *euc_status_string(int status) {
     case EUC_ERR_TIMEOUT: return "bounded device wait timed out";
     case EUC_ERR_BUDGET: return "request exceeds the framebuffer budget";
     case EUC_ERR_CAPACITY: return "input exceeds a fixed capacity";
+    case EUC_ERR_STALE: return "graph recorded against context scratch that has since moved";
     default: return "unknown status";
     }
 }
@@ -640,6 +686,28 @@ int euc_ctx_reserve(euc_ctx *ctx, uint64_t max_verts, uint64_t max_tris, uint64_
     if ((rc = grow(ctx->err, ns * sizeof(int)))) return rc;
     if ((rc = grow(ctx->stats, ns * sizeof(SceneStats)))) return rc;
     if ((rc = grow(ctx->cov, ns * sizeof(uint4)))) return rc;
+    if ((rc = grow(ctx->plan, 2 * (ns + 1) * sizeof(uint64_t)))) return rc;
+    return EUC_OK;
+}
+
+int euc_ctx_set_tuning(euc_ctx *ctx, const euc_tuning *t) {
+    if (!ctx) return EUC_ERR_INVALID;
+    euc_tuning v{};
+    if (t) {
+        v = *t;
+        if (v.raster_warp_rows && (v.raster_warp_rows % 32 || v.raster_warp_rows > (uint32_t)kWarpItems))
+            return EUC_ERR_INVALID;
+        if (v.raster_blocks_per_sm > 64 || v.chunk_group > 1024 || v.chunk_blocks_per_sm > 64) return EUC_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> g(ctx->mu);
+    ctx->tune = v;
+    return EUC_OK;
+}
+
+int euc_ctx_get_tuning(euc_ctx *ctx, euc_tuning *t) {
+    if (!ctx || !t) return EUC_ERR_INVALID;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    *t = ctx->tune;
     return EUC_OK;
 }
 
@@ -728,6 +796,118 @@ int euc_render_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, void *stre
     std::lock_guard<std::mutex> g(ctx->mu);
     CUDA_TRY(cudaSetDevice(ctx->device));
     return run_batch(ctx, scenes, n, (cudaStream_t)stream);
+}
+
+}  // extern "C"
+
+struct euc_graph {
+    euc_ctx *ctx = nullptr;
+    void *host = nullptr;  // staging owned by the graph: read by every replay
+    void *dev = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int nscenes = 0;
+    uint64_t launches = 0;   // kernels in the recorded batch
+    void *scratch[13] = {};  // the context's scratch pointers the graph was recorded with
+};
+
+namespace {
+
+// The scratch buffers a recorded batch reads and writes.  A later render that
+// grows one of them moves it, and the graph may then no longer be launched.
+constexpr int kScratchBufs = 13;
+void scratch_ptrs(const euc_ctx *c, void *out[kScratchBufs]) {
+    const DevBuf *b[kScratchBufs] = {&c->clip, &c->vdata,  &c->recs, &c->rows,  &c->chunk_sums,
+                                     &c->live_tri, &c->live_rowoff, &c->totals, &c->vbuf, &c->err,
+                                     &c->stats, &c->cov, &c->plan};
+    for (int i = 0; i < kScratchBufs; ++i) out[i] = b[i]->p;
+}
+
+void graph_free(euc_graph *g) {
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    if (g->host) cudaFreeHost(g->host);
+    if (g->dev) cudaFree(g->dev);
+    delete g;
+}
+
+}  // namespace
+
+extern "C" {
+
+int euc_graph_create(euc_ctx *ctx, const euc_scene *scenes, size_t n, euc_graph **out) {
+    if (!ctx || !out || (n && !scenes)) return EUC_ERR_INVALID;
+    *out = nullptr;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    CUDA_TRY(cudaSetDevice(ctx->device));
+    StageOverride so;
+    so.dry = true;
+    int rc = run_batch(ctx, scenes, n, nullptr, &so);  // validates, sizes the scratch
+    if (rc) return rc;
+    euc_graph *g = new (std::nothrow) euc_graph();
+    if (!g) return EUC_ERR_OOM;
+    g->ctx = ctx;
+    const size_t bytes = std::max<size_t>(so.need, 256);
+    if (cudaMallocHost(&g->host, bytes) != cudaSuccess || cudaMalloc(&g->dev, bytes) != cudaSuccess) {
+        (void)cudaGetLastError();
+        graph_free(g);
+        return EUC_ERR_OOM;
+    }
+    cudaStream_t cs = nullptr;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
+        (void)cudaGetLastError();
+        graph_free(g);
+        return EUC_ERR_CUDA;
+    }
+    so.dry = false;
+    so.host = g->host;
+    so.dev = g->dev;
+    so.need = bytes;
+    rc = EUC_ERR_CUDA;
+    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        ctx->capturing = true;
+        const uint64_t l0 = ctx->launches;
+        rc = run_batch(ctx, scenes, n, cs, &so);
+        g->launches = ctx->launches - l0;
+        ctx->launches = l0;
+        ctx->capturing = false;
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(cs, &graph);
+        g->graph = graph;
+        if (rc == EUC_OK && (ec != cudaSuccess || !graph)) rc = EUC_ERR_CUDA;
+    }
+    if (rc == EUC_OK && cudaGraphInstantiate(&g->exec, g->graph, 0) != cudaSuccess) rc = EUC_ERR_CUDA;
+    (void)cudaGetLastError();
+    cudaStreamDestroy(cs);
+    if (rc) {
+        graph_free(g);
+        return rc;
+    }
+    g->nscenes = ctx->last_nscenes;
+    scratch_ptrs(ctx, g->scratch);
+    *out = g;
+    return EUC_OK;
+}
+
+int euc_graph_launch(euc_graph *g, void *stream) {
+    if (!g || !g->exec) return EUC_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(g->ctx->mu);
+    void *now[kScratchBufs];
+    scratch_ptrs(g->ctx, now);
+    if (memcmp(now, g->scratch, sizeof(now)) != 0) return EUC_ERR_STALE;
+    CUDA_TRY(cudaSetDevice(g->ctx->device));
+    CUDA_TRY(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+    g->ctx->last_nscenes = g->nscenes;
+    g->ctx->launches += g->launches;
+    return EUC_OK;
+}
+
+int euc_graph_destroy(euc_graph *g) {
+    if (!g) return EUC_ERR_INVALID;
+    cudaSetDevice(g->ctx->device);
+    cudaDeviceSynchronize();
+    graph_free(g);
+    return EUC_OK;
 }
 
 int euc_render_host(euc_ctx *ctx, const euc_pipeline_desc *desc, const void *uniforms, size_t uniforms_size,
@@ -852,7 +1032,8 @@ constexpr size_t kNaStage = 4096;  // scene table, bases, uniforms
 constexpr size_t kNaOffErr = kNaStage;
 constexpr size_t kNaOffStats = kNaOffErr + 256;
 constexpr size_t kNaOffTotals = kNaOffStats + 256;
-constexpr size_t kNaOffCov = kNaOffTotals + 64;  // inside the 256-byte totals region
+constexpr size_t kNaOffCov = kNaOffTotals + 64;   // inside the 256-byte totals region
+constexpr size_t kNaOffPlan = kNaOffTotals + 128;  // k_plan's 2 x 2 chunk bases, same region
 constexpr size_t kNaOffClip = kNaOffTotals + 256;
 constexpr size_t kNaOffVdata = kNaOffClip + kNaMaxVerts * sizeof(float4);
 constexpr size_t kNaOffRecs = kNaOffVdata + kNaMaxVerts * kNaMaxNV * sizeof(float);
@@ -914,11 +1095,9 @@ void na_vertex_resolve(bool vertex, const SceneDev *sc, const uint64_t *base, ui
         k_vertex<F><<<(unsigned)nblk, kBlock, 0, st>>>(sc, base, 0, 1, 0, (float4 *)(a + kNaOffClip),
                                                        (float *)(a + kNaOffVdata));
     else
-        k_resolve<F><<<chunk_grid(nblk, t_na_nsm), kBlock, 0, st>>>(sc, base, 0, 1, 0, nblk,
-                                                                    chunk_group(nblk, t_na_nsm), (const TriRec *)(a + kNaOffRecs),
-                                                               (const float *)(a + kNaOffVdata),
-                                                               (const unsigned long long *)(a + kNaOffVbuf),
-                                                               (const uint4 *)(a + kNaOffCov));
+        k_resolve<F><<<chunk_grid(nblk, t_na_nsm), kBlock, 0, st>>>(
+            sc, base, 0, 1, chunk_group(nblk, t_na_nsm), (const TriRec *)(a + kNaOffRecs),
+            (const float *)(a + kNaOffVdata), (const unsigned long long *)(a + kNaOffVbuf), (const uint4 *)(a + kNaOffCov));
 }
 
 void na_dispatch(bool vertex, uint32_t shader, const SceneDev *sc, const uint64_t *base, uint64_t nblk,
@@ -1001,14 +1180,17 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
     k_scan<<<(unsigned)((tri + kScanBlock - 1) / kScanBlock), kBlock, 0, st>>>(
         (const uint32_t *)(a + kNaOffRows), (const uint2 *)(a + kNaOffChunks), tri, (uint32_t *)(a + kNaOffLiveTri),
         (uint64_t *)(a + kNaOffLiveOff), (unsigned long long *)(a + kNaOffTotals));
-    k_init<<<chunk_grid(pix / kBlock, nsm), kBlock, 0, st>>>(dsc, zero_base, 1, (const uint4 *)(a + kNaOffCov),
-                                                              (unsigned long long *)(a + kNaOffVbuf), pix / kBlock,
-                                                              chunk_group(pix / kBlock, nsm));
+    uint64_t *const ibase = (uint64_t *)(a + kNaOffPlan), *const rbase = ibase + 2;
+    k_plan<<<1, kBlock, 0, st>>>(dsc, 1, (const uint4 *)(a + kNaOffCov), ibase, rbase);
+    const uint64_t ichunks = (pix + kInitChunk - 1) / kInitChunk + 1;
+    k_init<<<chunk_grid(ichunks, nsm), kBlock, 0, st>>>(dsc, ibase, 1, (const uint4 *)(a + kNaOffCov),
+                                                         (unsigned long long *)(a + kNaOffVbuf),
+                                                         chunk_group(ichunks, nsm));
     k_raster<<<(unsigned)(nsm * raster_blocks_per_sm()), kBlock, 0, st>>>(
         dsc, (const TriRec *)(a + kNaOffRecs), (const uint32_t *)(a + kNaOffLiveTri), (const uint64_t *)(a + kNaOffLiveOff),
         (unsigned long long *)(a + kNaOffTotals), (const int *)(a + kNaOffErr),
-        (unsigned long long *)(a + kNaOffVbuf), (SceneStats *)(a + kNaOffStats), 0, nullptr);
-    na_dispatch(false, d.shader, dsc, zero_base, resolve_blocks(d), a, st);
+        (unsigned long long *)(a + kNaOffVbuf), (SceneStats *)(a + kNaOffStats), 0, nullptr, kWarpItems);
+    na_dispatch(false, d.shader, dsc, rbase, resolve_blocks(d), a, st);
     if (device_status)
         CUDA_TRY(cudaMemcpyAsync(device_status, a + kNaOffErr, sizeof(int), cudaMemcpyDeviceToDevice, st));
     CUDA_TRY(cudaGetLastError());

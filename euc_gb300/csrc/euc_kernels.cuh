@@ -429,19 +429,25 @@ EUC_DEV bool covered(const uint4 &c, uint32_t x, uint32_t y) {
     return x >= c.x && y >= c.y && x < ~c.z && y < ~c.w;
 }
 
-// Blocks of k_init / k_resolve walk groups of `group` consecutive 256-pixel
-// chunks, grid-strided, so the scene table is searched once per group rather
-// than once per chunk (the host picks group = 1 for small launches, up to
-// kChunkGroup for large batches).
+// Pixels of the covered rectangle [c.x, ~c.z) x [c.y, ~c.w); 0 when empty.
+__host__ __device__ inline uint64_t rect_area(const uint4 &c) {
+    const uint32_t x1 = ~c.z, y1 = ~c.w;
+    return (c.x < x1 && c.y < y1) ? (uint64_t)(x1 - c.x) * (y1 - c.y) : 0ull;
+}
+
+// Blocks of k_init / k_resolve walk groups of `group` consecutive chunks,
+// grid-strided, so the scene table is searched once per group rather than
+// once per chunk (the host picks group = 1 for small launches, up to
+// kChunkGroup for large batches).  The chunks of every scene are counted on
+// the device by k_plan, from the covered rectangle k_setup found, so no block
+// is spent on pixels that no primitive reaches.
 constexpr int kChunkGroup = 16;
 
-// Rows [y0, y1] of the pixels q0 .. q0+255 of a W-wide scene do not meet the
-// covered rectangle: the whole chunk can be skipped.
-EUC_DEV bool chunk_outside(const uint4 &c, uint64_t q0, uint32_t W) {
-    // pixel indices within a scene fit 32 bits (plan_scene checks W*H)
-    const uint32_t y0 = (uint32_t)q0 / W, y1 = ((uint32_t)q0 + kBlock - 1) / W;
-    return y1 < c.y || y0 >= ~c.w;
-}
+// Each thread of k_init initialises kInitPer entries of the covered rectangle
+// (their depth loads are in flight together); a chunk is kBlock * kInitPer
+// entries.
+constexpr int kInitPer = 4;
+constexpr int kInitChunk = kBlock * kInitPer;
 
 // Scene of chunk `c` given the scene of an earlier chunk of the same group.
 EUC_DEV int advance_scene(const uint64_t *base, int nsc, int si, uint64_t c) {
@@ -449,36 +455,59 @@ EUC_DEV int advance_scene(const uint64_t *base, int nsc, int si, uint64_t c) {
     return si;
 }
 
-__global__ void __launch_bounds__(kBlock) k_init(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ pix_base,
+// ibase: the first k_init chunk of every scene (nsc + 1 entries, k_plan).
+__global__ void __launch_bounds__(kBlock) k_init(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ ibase,
                                                  int nsc, const uint4 *__restrict__ cov,
-                                                 unsigned long long *__restrict__ vbuf, uint64_t nchunks,
-                                                 uint32_t group) {
+                                                 unsigned long long *__restrict__ vbuf, uint32_t group) {
     __shared__ int s_scene;
+    const uint64_t nchunks = ibase[nsc];
     for (uint64_t g = blockIdx.x; g * group < nchunks; g += gridDim.x) {
         const uint64_t c0 = g * group;
         __syncthreads();
-        if (threadIdx.x == 0) s_scene = find_scene(pix_base, nsc, c0 * kBlock);
+        if (threadIdx.x == 0) s_scene = find_scene(ibase, nsc, c0);
         __syncthreads();
         int si = s_scene;
         for (uint64_t c = c0; c < c0 + group && c < nchunks; ++c) {
-            const uint64_t pos = c * kBlock;
-            si = advance_scene(pix_base, nsc, si, pos);
+            si = advance_scene(ibase, nsc, si, c);
             const SceneDev &s = sc[si];
-            // ordered scenes initialise every entry: their pixel scan sums them all
-            const bool all = s.keytype == KEY_ORDERED;
-            if (!all && chunk_outside(cov[si], pos - s.pix_base, s.W)) continue;
-            const uint64_t q = pos + threadIdx.x - s.pix_base;
-            if (q >= (uint64_t)s.W * s.H) continue;
-            const uint32_t y = (uint32_t)q / s.W, x = (uint32_t)q - y * s.W;
-            if (!all && !covered(cov[si], x, y)) continue;
-            unsigned long long key = ~0ull;
+            const uint64_t i0 = (c - ibase[si]) * kInitChunk + (uint64_t)threadIdx.x * kInitPer;
+            unsigned long long *row0 = vbuf + s.pix_base;
             if (s.keytype == KEY_ORDERED) {
-                key = 0;  // no fragment yet, cursor 0
-            } else if (s.keytype == KEY_MIN) {
-                const float d0 = *reinterpret_cast<const float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x);
-                key = init_key_min(d0, s.depth_test == EUC_TEST_GREATER);
+                // every entry, padding included (the pixel scan sums them all):
+                // no fragment yet, cursor 0
+                const uint64_t lim = ((uint64_t)s.W * s.H + kBlock - 1) / kBlock * kBlock;
+                if (i0 < lim) {  // lim and i0 are multiples of kInitPer
+                    reinterpret_cast<ulonglong2 *>(row0 + i0)[0] = make_ulonglong2(0ull, 0ull);
+                    reinterpret_cast<ulonglong2 *>(row0 + i0)[1] = make_ulonglong2(0ull, 0ull);
+                }
+                continue;
             }
-            vbuf[s.pix_base + q] = key;
+            // entries i0 .. i0+3 of the covered rectangle, row by row
+            const uint4 cv = cov[si];
+            const uint64_t area = rect_area(cv);
+            if (i0 >= area) continue;
+            const uint32_t rw = ~cv.z - cv.x;
+            uint32_t y = (uint32_t)(i0 / rw);
+            uint32_t x = cv.x + (uint32_t)(i0 - (uint64_t)y * rw);
+            y += cv.y;
+            uint32_t px[kInitPer];
+            float d[kInitPer];
+#pragma unroll
+            for (int k = 0; k < kInitPer; ++k) {
+                const bool live = i0 + k < area;
+                px[k] = live ? y * s.W + x : 0xFFFFFFFFu;  // pixel indices fit 32 bits (plan_scene)
+                d[k] = (live && s.keytype == KEY_MIN)
+                           ? *reinterpret_cast<const float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x)
+                           : 0.0f;
+                if (++x == ~cv.z) {
+                    x = cv.x;
+                    ++y;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kInitPer; ++k)
+                if (px[k] != 0xFFFFFFFFu)
+                    row0[px[k]] = s.keytype == KEY_MIN ? init_key_min(d[k], s.depth_test == EUC_TEST_GREATER) : ~0ull;
         }
     }
 }
@@ -608,13 +637,14 @@ EUC_DEV void raster_row(const SceneDev &s, const TriRec &r, uint32_t t, uint32_t
     }
 }
 
-// Warps are scheduled independently: a warp claims the next kWarpItems
+// Warps are scheduled independently: a warp claims the next `witems`
 // (primitive, row) items from a global counter, finds the first primitive of
 // its range with a 32-way search of the row offsets, copies the offsets of
-// the (at most kWarpItems) primitives that the range can touch into shared
+// the (at most `witems`) primitives that the range can touch into shared
 // memory and maps each lane's items with a binary search there.  Rows of one
 // large primitive spread over many warps; no block barrier couples a warp to
-// the slowest row of another warp.
+// the slowest row of another warp.  witems: a multiple of 32, at most
+// kWarpItems (a launch-shape choice; results do not depend on it).
 constexpr int kWarpItems = 256;
 
 __global__ void __launch_bounds__(kBlock, 4) k_raster(const SceneDev *__restrict__ sc, const TriRec *__restrict__ recs,
@@ -623,7 +653,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_raster(const SceneDev *__restrict
                                                    unsigned long long *__restrict__ totals,
                                                    const int *__restrict__ err, unsigned long long *__restrict__ vbuf,
                                                    SceneStats *__restrict__ stats, int phase,
-                                                   uint2 *__restrict__ frags) {
+                                                   uint2 *__restrict__ frags, int witems) {
     __shared__ uint64_t s_off[kBlock / 32][kWarpItems];
     const int lane = threadIdx.x & 31;
     uint64_t *off = s_off[threadIdx.x >> 5];
@@ -631,10 +661,10 @@ __global__ void __launch_bounds__(kBlock, 4) k_raster(const SceneDev *__restrict
     // Warps beyond the number of chunks would only find the counter exhausted;
     // they leave at once instead of queueing on its atomic.
     const uint64_t gwarp = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5);
-    if (gwarp * kWarpItems >= nitems) return;
+    if (gwarp * witems >= nitems) return;
     for (;;) {
         unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(totals + 2 + phase, (unsigned long long)kWarpItems);
+        if (lane == 0) base = atomicAdd(totals + 2 + phase, (unsigned long long)witems);
         base = __shfl_sync(0xFFFFFFFFu, base, 0);
         if (base >= nitems) break;
         // largest l with live_rowoff[l] <= base; invariant off(lo) <= base < off(hi)
@@ -652,13 +682,13 @@ __global__ void __launch_bounds__(kBlock, 4) k_raster(const SceneDev *__restrict
             lo += 31 - __clz(__ballot_sync(0xFFFFFFFFu, le));
         }
         const uint64_t l0 = lo;
-        for (int j = lane; j < kWarpItems; j += 32) off[j] = l0 + j < nlive ? live_rowoff[l0 + j] : ~0ull;
+        for (int j = lane; j < witems; j += 32) off[j] = l0 + j < nlive ? live_rowoff[l0 + j] : ~0ull;
         __syncwarp();
         uint32_t scene0 = 0xFFFFFFFFu, cnt0 = 0;
-        for (int s = 0; s < kWarpItems / 32; ++s) {
+        for (int s = 0; s < witems / 32; ++s) {
             const uint64_t i = base + (uint64_t)s * 32 + lane;
             if (i >= nitems) break;
-            int a = 0, b = kWarpItems;  // the last window entry that starts at or before i
+            int a = 0, b = witems;  // the last window entry that starts at or before i
             while (b - a > 1) {
                 const int mid = (a + b) >> 1;
                 if (off[mid] <= i) a = mid; else b = mid;
@@ -737,24 +767,78 @@ EUC_DEV void store_pixel(const SceneDev &s, uint32_t x, uint32_t y, const float 
     }
 }
 
-// Row pairs of the level-1 coarse grid: the grid restarts at every band, so a
-// band of odd height ends with a single row.
-__host__ __device__ inline uint64_t quad_row_pairs(uint32_t H, uint32_t gr) {
-    const uint64_t nb = (H + gr - 1) / gr, ppb = (gr + 1) / 2, lh = H - (nb - 1) * gr;
-    return (nb - 1) * ppb + (lh + 1) / 2;
+// Level-1 MSAA scenes are resolved by warps of 16x2 pixels that cover whole
+// 2x2 cells of the band-relative coarse grid: row pair p = b * ppb + k is rows
+// b*gr + 2k and b*gr + 2k + 1 of band b (a band of odd height ends with a
+// single row), ppb = ceil(gr / 2).
+__host__ __device__ inline uint32_t pair_of_row(uint32_t y, uint32_t gr) {
+    return (y / gr) * ((gr + 1) >> 1) + ((y % gr) >> 1);
 }
 
 __host__ __device__ inline bool resolve_by_quads(const SceneDev &s) {
     return s.level == 1 && s.pixel_write && s.keytype != KEY_ORDERED;
 }
 
-// Blocks of k_resolve for one scene.
-__host__ __device__ inline uint64_t resolve_blocks(const SceneDev &s) {
+// k_resolve chunks (blocks of work) of a scene: kBlock pixels of the covered
+// rectangle, or kBlock/32 warp tiles of 16x2 pixels over the row pairs and
+// 16-pixel columns that meet it.
+__host__ __device__ inline uint64_t resolve_chunks(const SceneDev &s, const uint4 &cv) {
+    const uint64_t area = rect_area(cv);
+    if (area == 0) return 0;
     if (resolve_by_quads(s)) {
-        const uint64_t warps = quad_row_pairs(s.H, s.gr) * ((s.W + 15) / 16);
-        return (warps + kBlock / 32 - 1) / (kBlock / 32);
+        const uint64_t pairs = pair_of_row(~cv.w - 1, s.gr) - pair_of_row(cv.y, s.gr) + 1;
+        const uint64_t cols = ((~cv.z - 1) >> 4) - (cv.x >> 4) + 1;
+        return (pairs * cols + kBlock / 32 - 1) / (kBlock / 32);
     }
-    return ((uint64_t)s.W * s.H + kBlock - 1) / kBlock;
+    return (area + kBlock - 1) / kBlock;
+}
+
+// Upper bound of resolve_chunks over every rectangle (the whole target), for
+// sizing launches on the host.
+__host__ __device__ inline uint64_t resolve_blocks(const SceneDev &s) {
+    uint4 full;
+    full.x = 0;
+    full.y = 0;
+    full.z = ~s.W;
+    full.w = ~s.H;
+    return resolve_chunks(s, full);
+}
+
+// Chunk bases of k_init and k_resolve per scene, from the covered rectangles
+// (exclusive prefix sums, nsc + 1 entries each).  One block, any nsc.
+__global__ void __launch_bounds__(kBlock) k_plan(const SceneDev *__restrict__ sc, int nsc,
+                                                 const uint4 *__restrict__ cov, uint64_t *__restrict__ ibase,
+                                                 uint64_t *__restrict__ rbase) {
+    __shared__ uint64_t s_a[kBlock / 32 + 1];
+    uint64_t ci = 0, cr = 0;
+    for (int s0 = 0; s0 < nsc; s0 += kBlock) {
+        const int si = s0 + (int)threadIdx.x;
+        uint64_t ni = 0, nr = 0;
+        if (si < nsc) {
+            const SceneDev &s = sc[si];
+            const uint4 cv = cov[si];
+            if (s.keytype == KEY_ORDERED) {  // every entry; k_resolve_ordered sizes itself
+                const uint64_t lim = ((uint64_t)s.W * s.H + kBlock - 1) / kBlock * kBlock;
+                ni = (lim + kInitChunk - 1) / kInitChunk;
+            } else {
+                ni = (rect_area(cv) + kInitChunk - 1) / kInitChunk;
+                nr = resolve_chunks(s, cv);
+            }
+        }
+        uint64_t ti, tr;
+        const uint64_t ei = block_excl_scan<uint64_t>(ni, s_a, &ti);
+        const uint64_t er = block_excl_scan<uint64_t>(nr, s_a, &tr);
+        if (si < nsc) {
+            ibase[si] = ci + ei;
+            rbase[si] = cr + er;
+        }
+        ci += ti;
+        cr += tr;
+    }
+    if (threadIdx.x == 0) {
+        ibase[nsc] = ci;
+        rbase[nsc] = cr;
+    }
 }
 
 template <class F>
@@ -772,37 +856,55 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
                            const float *__restrict__ vdata, const unsigned long long *__restrict__ vbuf,
                            ResolveSmem<F> &sm) {
     const int tid = threadIdx.x, lane = tid & 31;
-    // 1. this thread's pixel
+    // 1. this thread's pixel: chunk lb of the covered rectangle (it is not
+    // empty, or the scene would have no chunks)
     uint32_t x = 0, y = 0, lo = 0;
     bool inside;
     const bool quads = resolve_by_quads(s);
     if (quads) {  // warp = 16x2 pixels on whole 2x2 cells of the band-relative grid
-        const uint32_t cols = (s.W + 15) >> 4, ppb = (s.gr + 1) >> 1;
+        const uint32_t ppb = (s.gr + 1) >> 1;
+        const uint32_t p0 = pair_of_row(cv.y, s.gr), a0 = cv.x >> 4;
+        const uint32_t cols = ((~cv.z - 1) >> 4) - a0 + 1;
+        const uint64_t npairs = pair_of_row(~cv.w - 1, s.gr) - p0 + 1;
         const uint64_t w = lb * (kBlock / 32) + (tid >> 5);
-        inside = w < quad_row_pairs(s.H, s.gr) * cols;
+        inside = w < npairs * cols;
         if (inside) {
-            const uint32_t p = (uint32_t)(w / cols), a = (uint32_t)(w % cols);
+            const uint32_t p = p0 + (uint32_t)(w / cols), a = a0 + (uint32_t)(w % cols);
             const uint32_t b = p / ppb, k = p % ppb;
             lo = b * s.gr;
             x = a * 16 + (lane & 15);
             y = lo + 2 * k + (lane >> 4);
-            inside = x < s.W && y < min(lo + s.gr, s.H);
+            inside = x < s.W && y < min(lo + s.gr, s.H) && covered(cv, x, y);
         }
     } else {
-        const uint64_t q = lb * kBlock + tid;
-        inside = q < (uint64_t)s.W * s.H;
+        const uint32_t rw = ~cv.z - cv.x;
+        const uint64_t i = lb * kBlock + tid;
+        inside = i < rect_area(cv);
         if (inside) {
-            y = (uint32_t)q / s.W;
-            x = (uint32_t)q - y * s.W;
+            const uint32_t ry = (uint32_t)(i / rw);
+            y = cv.y + ry;
+            x = cv.x + (uint32_t)(i - (uint64_t)ry * rw);
             lo = (y / s.gr) * s.gr;
         }
     }
-    inside = inside && covered(cv, x, y);  // no primitive reaches other pixels
     uint32_t t = 0xFFFFFFFFu;
     float z = 0.0f;
     const bool win = inside && decode_key(s, vbuf[s.pix_base + (uint64_t)y * s.W + x], t, z);
     if (win && s.depth_write) *reinterpret_cast<float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x) = z;
     if (!s.pixel_write) return;  // uniform over the block (one scene)
+    if (F::kDirect && s.level == 0) {
+        // a cheap shader without MSAA: each winner is shaded where it is
+        if (!win) return;
+        const typename F::U &u = *reinterpret_cast<const typename F::U *>(s.uniforms);
+        const float *vb = vdata + s.vd_base;
+        const TriRec &r = recs[t];
+        float vd[F::NV], frag[F::NF];
+        get_v_data<F>(r, vb + (uint64_t)r.v[0] * F::NV, vb + (uint64_t)r.v[1] * F::NV, vb + (uint64_t)r.v[2] * F::NV,
+                      (float)x, (float)y, vd);
+        F::fragment(u, vd, frag);
+        store_pixel<F>(s, x, y, frag);
+        return;
+    }
     if (!__syncthreads_or(win)) return;  // nothing to shade in this chunk
 
     // 2. the fragment evaluations this chunk needs, compacted into a job list.
@@ -890,32 +992,29 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
     store_pixel<F>(s, x, y, frag);
 }
 
-// Blocks walk groups of kChunkGroup chunks (grid-strided); the chunk of each
-// scene are [res_base[s], res_base[s] + resolve_blocks(s)).
+// Blocks walk groups of `group` chunks (grid-strided) of the scenes
+// [s_begin, s_end); rbase (global scene index, from k_plan) holds the first
+// chunk of each.
 template <class F>
-__global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ res_base,
-                                                    int s_begin, int s_end, uint64_t blk_begin, uint64_t nblk,
-                                                    uint32_t group, const TriRec *__restrict__ recs,
-                                                    const float *__restrict__ vdata,
+__global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ rbase,
+                                                    int s_begin, int s_end, uint32_t group,
+                                                    const TriRec *__restrict__ recs, const float *__restrict__ vdata,
                                                     const unsigned long long *__restrict__ vbuf,
                                                     const uint4 *__restrict__ cov) {
     __shared__ ResolveSmem<F> sm;
     __shared__ int s_scene;
-    const uint64_t *base = res_base + s_begin;
+    const uint64_t *base = rbase + s_begin;
     const int n = s_end - s_begin;
-    for (uint64_t g = blockIdx.x; g * group < nblk; g += gridDim.x) {
-        const uint64_t c0 = blk_begin + g * group;
+    const uint64_t c_begin = base[0], c_end = base[n];
+    for (uint64_t g = blockIdx.x; c_begin + g * group < c_end; g += gridDim.x) {
+        const uint64_t c0 = c_begin + g * group;
         __syncthreads();
         if (threadIdx.x == 0) s_scene = find_scene(base, n, c0);
         __syncthreads();
         int si = s_scene;
-        for (uint64_t c = c0; c < c0 + group && c < blk_begin + nblk; ++c) {
+        for (uint64_t c = c0; c < c0 + group && c < c_end; ++c) {
             si = advance_scene(base, n, si, c);
-            const SceneDev &s = sc[s_begin + si];
-            const uint4 cv = cov[s_begin + si];
-            const uint64_t lb = c - base[si];
-            if (!resolve_by_quads(s) && chunk_outside(cv, lb * kBlock, s.W)) continue;  // uniform
-            resolve_chunk<F>(s, cv, lb, recs, vdata, vbuf, sm);
+            resolve_chunk<F>(sc[s_begin + si], cov[s_begin + si], c - base[si], recs, vdata, vbuf, sm);
             __syncthreads();  // the next chunk reuses shared memory
         }
     }

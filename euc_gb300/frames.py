@@ -238,5 +238,26 @@ def render_batch(ctx, dframes, stream=None, clear=True):
         del keep
 
 
+class BatchGraph:
+    """A DeviceBatch recorded as one euc_graph per pass; `launch` clears the
+    targets (two fills) and replays the passes in order."""
+
+    def __init__(self, ctx, batch):
+        self.batch = batch
+        self.graphs = [ctx.graph(arr) for arr in batch.scene_arrays()]
+
+    def launch(self, stream=None, clear=True):
+        if clear:
+            self.batch.clear()
+        sp = _stream_ptr(stream)
+        for g in self.graphs:
+            g.launch(sp)
+
+    def close(self):
+        for g in self.graphs:
+            g.close()
+        self.graphs = []
+
+
 def frame_stats(ctx, stream=None):
     return ctx.stats(_stream_ptr(stream))

@@ -11,7 +11,9 @@ Generators (all deterministic in `seed`, numpy PCG64):
                     RGBA8 colour (the fill-rate scene);
   * knot_frame    — (2,3) torus knot, shadow-map pass + textured Phong pass
                     with coarse-grid MSAA (the two-pass scene);
-  * batch_frames  — many independent scenes of uneven size for the batched form.
+  * batch_frames  — many independent scenes of uneven size for the batched form;
+  * serve_assets / serve_frame — resident meshes and textures, and two-pass
+                    requests over them for the serving loop.
 """
 from dataclasses import dataclass, field
 import ctypes as C
@@ -512,3 +514,63 @@ def batch_frames(seed=0, n=256, tri_lo=100, tri_hi=100_000, resolutions=(64, 128
                                  TargetSpec("depth", res, res, abi.FMT_R32F, 1.0)], [p],
                                 {"seed": seed, "kind": kind, "index": s}))
     return frames
+
+
+@dataclass
+class ServeAssets:
+    """Resident inputs of the serving workload: meshes (packed vertex buffer,
+    layout, vertex count, u32 indices) and RGBA8 textures."""
+    meshes: list
+    textures: list
+
+
+def serve_assets(seed=0, nmeshes=64, ntextures=32, tex_size=512, tri_lo=100, tri_hi=100_000):
+    """`nmeshes` meshes from the batch generators (sphere / torus knot / soup,
+    triangle counts log-uniform in [tri_lo, tri_hi], pos+normal+uv f32) and
+    `ntextures` tex_size^2 RGBA8 value-noise textures."""
+    rng = np.random.default_rng(seed)
+    meshes = []
+    for m in range(nmeshes):
+        kind = ("sphere", "knot", "soup")[int(rng.integers(0, 3))]
+        nt = int(round(math.exp(rng.uniform(math.log(tri_lo), math.log(tri_hi)))))
+        pos, nrm, uv, idx = _mesh_for(kind, nt, rng)
+        buf, stride, offs = pack_vertices(pos, nrm, uv)
+        meshes.append({"kind": kind, "vertices": buf, "nverts": len(pos), "indices": idx,
+                       "layout": layout(stride, position=offs[0], normal=offs[1], uv=offs[2])})
+    textures = [value_noise_texture(rng, tex_size, cells=8) for _ in range(ntextures)]
+    return ServeAssets(meshes, textures)
+
+
+def serve_frame(assets, rng, resolutions=(64, 128, 256, 512), band_rows=abi.BANDS_PAR):
+    """One serving request as a FrameSpec: a resident mesh and texture drawn
+    uniformly, a square resolution from `resolutions`, Msaa{level: 1} for
+    half, a seeded camera and spotlight.  Two passes as in the two-pass
+    shadow-mapped configuration: a res^2 f32 shadow map from the light
+    (PixelMode::PASS, LESS_WRITE, no culling), then textured Phong with the
+    shadow map into RGBA8 + f32 depth."""
+    mi = int(rng.integers(0, len(assets.meshes)))
+    ti = int(rng.integers(0, len(assets.textures)))
+    res = int(resolutions[int(rng.integers(0, len(resolutions)))])
+    aa = int(rng.integers(0, 2))
+    m = assets.meshes[mi]
+    model = quat_rotation(rng)
+    view = translation(0, 0, 3.2)
+    proj = perspective_lh_zo(1.0, 1.0, 0.05, 50.0)
+    light_pos = rng.uniform(-3, 3, 3) + np.array([-6.0, 5.0, -5.0])
+    light_vp = perspective_lh_zo(0.9, 1.0, 0.1, 100.0) @ look_at_lh(light_pos, [0, 0, 0], [0, 1, 0])
+    su = abi.ShadowUniforms()
+    su.mvp = f32mat(light_vp @ model)
+    shadow_pass = PassSpec(make_desc(abi.SHADER_SHADOW, pixel_write=0, cull=abi.CULL_NONE, band_rows=band_rows),
+                           m["layout"], m["vertices"], m["nverts"], m["indices"], su, pixel=None, depth="shadow")
+    cull = abi.CULL_NONE if m["kind"] == "soup" else abi.CULL_BACK
+    pu = _phong_uniforms(model, view, proj, light_vp, light_pos, np.linalg.inv(view)[:3, 3])
+    color_pass = PassSpec(make_desc(abi.SHADER_PHONG, aa_level=aa, cull=cull, band_rows=band_rows),
+                          m["layout"], m["vertices"], m["nverts"], m["indices"], pu,
+                          [SamplerSpec("tex", assets.textures[ti], abi.FILTER_LINEAR, abi.WRAP_TILE, 255.0),
+                           SamplerSpec("shadow", "shadow", abi.FILTER_LINEAR, abi.WRAP_CLAMP, 1.0)],
+                          pixel="color", depth="depth")
+    return FrameSpec("serve_m%d_t%d_%d_aa%d" % (mi, ti, res, aa),
+                     [TargetSpec("shadow", res, res, abi.FMT_R32F, 1.0),
+                      TargetSpec("color", res, res, abi.FMT_RGBA8, 0),
+                      TargetSpec("depth", res, res, abi.FMT_R32F, 1.0)],
+                     [shadow_pass, color_pass], {"mesh": mi, "texture": ti, "kind": "serve"})

@@ -39,7 +39,9 @@ enum euc_status {
                                   at pipeline.rs:330                                    */
     EUC_ERR_TIMEOUT = 7,       /* a bounded device wait ran out                          */
     EUC_ERR_BUDGET = 8,        /* serving: request larger than the framebuffer budget    */
-    EUC_ERR_CAPACITY = 9       /* a fixed-capacity variant was given more than it holds  */
+    EUC_ERR_CAPACITY = 9,      /* a fixed-capacity variant was given more than it holds  */
+    EUC_ERR_STALE = 10,        /* a recorded graph whose context scratch has since moved */
+    EUC_ERR_BUSY = 11          /* serving: the admission queue is full                   */
 };
 
 /* DepthMode.test (pipeline.rs:14-19): Option<Ordering>, compared with
@@ -254,6 +256,18 @@ enum euc_stage {
     EUC_STAGE_COUNT = 6
 };
 
+/* Launch shape of the pipeline (no counterpart in euc).  None of these
+ * changes a result, only how work is spread over the GPU; 0 keeps the
+ * default.  Set by an autotuner that times a batch under several shapes.   */
+typedef struct euc_tuning {
+    uint32_t raster_blocks_per_sm; /* persistent k_raster blocks per SM (default: occupancy limit) */
+    uint32_t raster_warp_rows;     /* (primitive, row) items a warp claims at once, 32..256, x32 (256) */
+    uint32_t chunk_group;          /* 256-pixel chunks per scene lookup in init/resolve (adaptive)   */
+    uint32_t chunk_blocks_per_sm;  /* init/resolve grid cap per SM (16)                              */
+} euc_tuning;
+int euc_ctx_set_tuning(euc_ctx *ctx, const euc_tuning *tuning);
+int euc_ctx_get_tuning(euc_ctx *ctx, euc_tuning *tuning);
+
 /* Profiling aid (no counterpart in euc): while enabled, each render records
  * CUDA events around its stages on its own stream.  euc_ctx_profile waits for
  * them, returns the summed milliseconds per stage and the number of kernel
@@ -288,6 +302,23 @@ int euc_render_host(euc_ctx *ctx, const euc_pipeline_desc *desc, const void *uni
  * rendered alone with euc_render.  No counterpart in euc.                   */
 int euc_render_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, void *stream);
 
+/* A batch recorded once as a CUDA graph and replayed with one launch.  The
+ * graph holds the scene table, the uniforms and every device pointer of
+ * `scenes` as they were at creation: between launches the caller may change
+ * the contents of vertex, index, texture and target buffers, not the
+ * pointers or sizes.  It renders with `ctx`'s scratch buffers, so its
+ * launches must be ordered with every other render on that context.  A later
+ * render on the context that needs more scratch than the context held at
+ * creation moves that scratch; the graph then refuses to launch
+ * (EUC_ERR_STALE) and must be recreated (euc_ctx_reserve before creation
+ * avoids that).  Destroy graphs before their context.  Scenes on the ordered
+ * path (EUC_BLEND_ALPHA, EUC_FLAG_ORDERED) cannot be recorded
+ * (EUC_ERR_INVALID).  No counterpart in euc.                                */
+typedef struct euc_graph euc_graph;
+int euc_graph_create(euc_ctx *ctx, const euc_scene *scenes, size_t n, euc_graph **out);
+int euc_graph_launch(euc_graph *graph, void *stream);
+int euc_graph_destroy(euc_graph *graph);
+
 /* euc_render without a context and without any allocation.  No counterpart in
  * euc: it exists for callers that may not allocate device memory, such as an
  * engine or plugin host that owns a fixed device-memory budget, or a render
@@ -307,6 +338,123 @@ int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uniforms, size
                        const euc_vertex_layout *layout, const void *vertices, size_t nverts,
                        const uint32_t *indices, size_t nindices, const euc_target *pixel,
                        const euc_target *depth, void *stream, int *device_status);
+
+/* ---- serving (no counterpart in euc) ------------------------------------
+ *
+ * A request loop on one device.  Meshes and textures are uploaded once and
+ * stay resident; each request names them by id, brings its uniforms and
+ * lists its targets (framebuffers), which the server carves out of a fixed
+ * device-memory budget when it admits the request.  A serving thread admits
+ * requests in submission order as soon as their arrival time has passed and
+ * the budget has room, gathers whatever is admissible into a batch when one
+ * of its `slots` (a stream with its own euc_ctx) is free, and runs the batch
+ * as euc_render_batch calls (pass k of every request in the k-th call; the
+ * passes of one request stay in order), so batches of several slots overlap
+ * on the device while new requests keep arriving.  Each request's targets are
+ * cleared to their clear value first; after the last pass, targets marked
+ * `readback` are copied to the request's `out` buffer and the request
+ * completes.  Every image is byte-identical to the same passes rendered with
+ * euc_render on targets cleared the same way.                               */
+typedef struct euc_server euc_server;
+
+typedef struct euc_server_config {
+    int32_t device;
+    uint32_t max_batch;          /* requests per batch (0: 256)                         */
+    uint64_t framebuffer_budget; /* device bytes for the targets of admitted requests   */
+    uint32_t slots;              /* batches in flight, one stream + context each (0: 3) */
+    uint32_t max_pending;        /* submitted, not yet admitted requests (0: 1 << 20)   */
+} euc_server_config;
+
+typedef struct euc_server_target {
+    uint32_t width, height;
+    uint32_t format;   /* euc_format                                                   */
+    uint32_t clear;    /* colour: little-endian packed texel; R32F: the f32 bit pattern */
+    uint32_t readback; /* non-zero: copied to the request's `out` on completion         */
+    uint32_t reserved;
+} euc_server_target;
+
+/* Points the euc_sampler at byte `offset` of a pass's uniforms at a resident
+ * texture (`texture` >= 0) or at one of the request's own targets written by
+ * an earlier pass (`target` >= 0).  The sampler keeps its filter, wrap and
+ * texel_div; its data, width, height, pitch and format are set here.        */
+typedef struct euc_server_binding {
+    uint32_t offset;
+    int32_t texture;
+    int32_t target;
+    uint32_t reserved;
+} euc_server_binding;
+
+typedef struct euc_server_pass {
+    euc_pipeline_desc desc;
+    uint32_t mesh;         /* resident mesh id                                      */
+    int32_t pixel_target;  /* index into the request's targets, -1: Empty           */
+    int32_t depth_target;  /* index into the request's targets, -1: Empty           */
+    uint32_t nbindings;
+    const euc_server_binding *bindings;
+    const void *uniforms;  /* the shader's uniform struct (copied at submission)    */
+    uint64_t uniforms_size;
+} euc_server_pass;
+
+#define EUC_SERVER_MAX_TARGETS 4
+#define EUC_SERVER_MAX_PASSES 4
+
+typedef struct euc_server_request {
+    uint64_t tag;        /* returned with the completion                              */
+    uint64_t arrival_ns; /* euc_server_now_ns() time from which it may be admitted; 0: now */
+    void *out;           /* host memory for the readback targets, in target order,
+                            rows of width * bytes-per-texel; page-locked memory keeps
+                            the copy asynchronous                                     */
+    uint64_t out_size;
+    uint32_t ntargets, npasses;
+    const euc_server_target *targets;
+    const euc_server_pass *passes;
+} euc_server_request;
+
+typedef struct euc_server_completion {
+    uint64_t id, tag;
+    int32_t status;
+    uint32_t batch_size;  /* requests in the batch it ran in                            */
+    uint64_t arrival_ns;  /* the request's arrival (its submission time if it gave 0)   */
+    uint64_t admit_ns;    /* admitted into a batch                                      */
+    uint64_t done_ns;     /* its batch finished on the device, readback included        */
+} euc_server_completion;
+
+typedef struct euc_server_stats {
+    uint64_t submitted, completed, failed, refused;
+    uint64_t pending, in_flight;
+    uint64_t batches, batched_requests;
+    uint64_t budget_bytes, budget_used, budget_peak;
+    uint64_t launches;  /* kernels launched so far (target clears + renders)      */
+} euc_server_stats;
+
+int euc_server_create(const euc_server_config *config, euc_server **out);
+/* Waits for the batches in flight, drops requests not yet admitted.         */
+int euc_server_destroy(euc_server *srv);
+/* Uploads a mesh (host vertices of nverts * layout->stride bytes, u32 indices
+ * or NULL) and returns its id; indices are checked against nverts here.     */
+int euc_server_add_mesh(euc_server *srv, const euc_vertex_layout *layout, const void *vertices, size_t nverts,
+                        const uint32_t *indices, size_t nindices, uint32_t *id);
+/* Uploads a texture (RGBA8 or R32F, the sampler formats; rows `pitch` bytes
+ * apart on the host, packed on the device) and returns its id.             */
+int euc_server_add_texture(euc_server *srv, const void *texels, uint32_t width, uint32_t height, uint64_t pitch,
+                           uint32_t format, uint32_t *id);
+/* Nanoseconds of a steady clock since the server was created.               */
+uint64_t euc_server_now_ns(euc_server *srv);
+/* Queues `n` requests with consecutive ids from *first_id.  Every request is
+ * checked first (ids, target indices, sizes, uniforms, `out` size); if one
+ * fails, none is queued (EUC_ERR_INVALID, or EUC_ERR_BUDGET for a request
+ * whose targets alone exceed the budget).  When the admission queue holds
+ * max_pending requests the rest are refused: *accepted says how many were
+ * queued and the call returns EUC_ERR_BUSY.                                 */
+int euc_server_submit(euc_server *srv, const euc_server_request *reqs, size_t n, uint64_t *first_id,
+                      size_t *accepted);
+/* Moves up to `max` completions into `out`, waiting up to `wait_ms` for the
+ * first one (0: no wait).                                                   */
+int euc_server_poll(euc_server *srv, euc_server_completion *out, size_t max, size_t *n, int wait_ms);
+/* Waits until nothing is pending or in flight (EUC_ERR_TIMEOUT after
+ * `timeout_ms`, < 0: no limit).                                             */
+int euc_server_drain(euc_server *srv, int timeout_ms);
+int euc_server_stats_get(euc_server *srv, euc_server_stats *out);
 
 #ifdef __cplusplus
 }

@@ -19,6 +19,10 @@ STRUCTS = {
     "euc_vcolor_uniforms": abi.VColorUniforms, "euc_gouraud_uniforms": abi.GouraudUniforms,
     "euc_textured_uniforms": abi.TexturedUniforms, "euc_phong_uniforms": abi.PhongUniforms,
     "euc_shadow_uniforms": abi.ShadowUniforms, "euc_stats": abi.Stats, "euc_scene": abi.Scene,
+    "euc_tuning": abi.Tuning, "euc_server_config": abi.ServerConfig, "euc_server_target": abi.ServerTarget,
+    "euc_server_binding": abi.ServerBinding, "euc_server_pass": abi.ServerPass,
+    "euc_server_request": abi.ServerRequest, "euc_server_completion": abi.ServerCompletion,
+    "euc_server_stats": abi.ServerStats,
 }
 
 
