@@ -427,6 +427,9 @@ def run_gpu(args):
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": alg_bytes,
                          "traffic": traffic.get(args.workload, {}).get("k_" + dom) if traffic else None},
+            # the whole step (every stage, launch gaps included) against the same peak
+            "pipeline_roofline": {"achieved": alg_bytes / (ms_step / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                                  "frac": alg_bytes / (ms_step / 1e3) / 1e9 / peak, "peak_kind": peak_kind},
             "e2e": {"value": e2e, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "path": "euc_render_host per scene (host buffers, blocking)"},
             "cpu_baseline": cpu,

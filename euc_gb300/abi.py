@@ -31,6 +31,8 @@ STATUS_NAMES = {
 }
 
 TEST_NONE, TEST_LESS, TEST_EQUAL, TEST_GREATER = 0, 1, 2, 3
+PRIM_TRIANGLE_LIST, PRIM_LINE_TRIANGLE_LIST, PRIM_LINE_LIST = 0, 1, 2
+SRC_RGBA8, SRC_BGRA8, SRC_RGB8, SRC_LUMA8, SRC_LUMA_ALPHA8, SRC_R32F = 0, 1, 2, 3, 4, 5
 CULL_NONE, CULL_BACK, CULL_FRONT = 0, 1, 2
 Y_DOWN, Y_UP = 0, 1
 LEFT, RIGHT = 0, 1
@@ -56,7 +58,7 @@ class PipelineDesc(C.Structure):
         ("depth_write", C.c_uint32), ("handedness", C.c_uint32), ("y_axis", C.c_uint32),
         ("z_clip", C.c_uint32), ("z_clip_min", C.c_float), ("z_clip_max", C.c_float),
         ("aa_level", C.c_uint32), ("cull", C.c_uint32), ("blend", C.c_uint32),
-        ("band_rows", C.c_uint32), ("flags", C.c_uint32),
+        ("band_rows", C.c_uint32), ("flags", C.c_uint32), ("primitives", C.c_uint32),
     ]
 
 
@@ -119,7 +121,7 @@ class Stats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("raster_blocks_per_sm", C.c_uint32), ("raster_warp_rows", C.c_uint32),
-                ("chunk_group", C.c_uint32), ("chunk_blocks_per_sm", C.c_uint32)]
+                ("chunk_group", C.c_uint32), ("chunk_blocks_per_sm", C.c_uint32), ("raster_probe", C.c_uint32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

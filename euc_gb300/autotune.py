@@ -2,8 +2,9 @@
 
 `euc_ctx_set_tuning` changes how a batch is spread over the GPU: persistent
 raster blocks per SM, the (primitive, row) items a raster warp claims at a
-time, and the chunk grouping and grid cap of the init/resolve kernels.  None
-of these changes a result.  The tuner times a `frames.DeviceBatch` under a set
+time, whether the raster reads a key before its atomicMin, and the chunk
+grouping and grid cap of the init/resolve kernels.  None of these changes a
+result.  The tuner times a `frames.DeviceBatch` under a set
 of candidate shapes (coordinate descent: the raster knobs first, then the
 chunk knobs), checks that every candidate's targets are byte-identical to the
 default shape's, keeps the fastest and caches the choice per device and
@@ -24,6 +25,7 @@ RASTER_BLOCKS = (0, 2, 3)          # 0: the occupancy limit
 RASTER_WARP_ROWS = (256, 128, 64)
 CHUNK_GROUP = (0, 1, 4, 16)        # 0: adaptive
 CHUNK_BLOCKS = (0, 8, 32)          # 0: 16 per SM
+RASTER_PROBE = (0, 1)              # 0: atomics only; 1: read keys before their atomics
 
 
 def workload_key(batch):
@@ -93,14 +95,15 @@ def tune(ctx, batch, stream=None, reps=5, cache=CACHE, verify=True, log=None):
             log("autotune %s: %.3f ms" % (cand, ms))
         return ms
 
-    best = {"raster_blocks_per_sm": 0, "raster_warp_rows": 0, "chunk_group": 0, "chunk_blocks_per_sm": 0}
+    best = {k: 0 for k, _ in abi.Tuning._fields_}
     default_ms = best_ms = run(best)
-    for rb in RASTER_BLOCKS:
-        for wr in RASTER_WARP_ROWS:
-            cand = dict(best, raster_blocks_per_sm=rb, raster_warp_rows=wr)
-            ms = run(cand)
-            if ms < best_ms:
-                best, best_ms = cand, ms
+    for pr in RASTER_PROBE:
+        for rb in RASTER_BLOCKS:
+            for wr in RASTER_WARP_ROWS:
+                cand = dict(best, raster_probe=pr, raster_blocks_per_sm=rb, raster_warp_rows=wr)
+                ms = run(cand)
+                if ms < best_ms:
+                    best, best_ms = cand, ms
     for cg in CHUNK_GROUP:
         for cb in CHUNK_BLOCKS:
             cand = dict(best, chunk_group=cg, chunk_blocks_per_sm=cb)

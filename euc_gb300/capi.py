@@ -47,6 +47,10 @@ SIGNATURES = {
                                   C.c_int]),
     "euc_server_drain": (C.c_int, [C.c_void_p, C.c_int]),
     "euc_server_stats_get": (C.c_int, [C.c_void_p, C.POINTER(abi.ServerStats)]),
+    "euc_texture_ingest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32,
+                                     C.c_void_p, C.c_uint64, C.c_void_p]),
+    "euc_sample_nearest": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.c_uint32, C.c_uint32,
+                                     C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
     "euc_render_noalloc": (C.c_int, [C.POINTER(abi.PipelineDesc), C.c_void_p, C.c_size_t, C.POINTER(abi.VertexLayout),
                                      C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(abi.Target),
                                      C.POINTER(abi.Target), C.c_void_p, C.c_void_p]),

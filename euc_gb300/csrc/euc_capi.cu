@@ -154,7 +154,7 @@ int plan_scene(const euc_scene &sc, Plan &p) {
     const euc_pipeline_desc &d = sc.desc;
     if (d.shader >= EUC_SHADER_COUNT) return EUC_ERR_INVALID;
     if (d.depth_test > EUC_TEST_GREATER || d.cull > EUC_CULL_FRONT || d.y_axis > EUC_Y_UP) return EUC_ERR_INVALID;
-    if (d.blend > EUC_BLEND_ALPHA) return EUC_ERR_INVALID;
+    if (d.blend > EUC_BLEND_ALPHA || d.primitives > EUC_PRIM_LINE_LIST) return EUC_ERR_INVALID;
     const size_t need = uniforms_size_for(d.shader);
     if (!sc.uniforms || sc.uniforms_size < need) return EUC_ERR_INVALID;
     const euc_vertex_layout &l = sc.layout;
@@ -224,7 +224,7 @@ int plan_scene(const euc_scene &sc, Plan &p) {
     if (W == 0 || H == 0) { p.skip = true; return EUC_OK; }
     if ((uint64_t)W * H >= 0xFFFFFF00ull) return EUC_ERR_CAPACITY;  // pixel indices are 32-bit on the device
     const uint64_t nstream = sc.indices ? sc.nindices : sc.nverts;
-    if (sc.nverts >= 0xFFFFFFFFull || nstream / 3 >= 0x3FFFFFFFull) return EUC_ERR_INVALID;
+    if (sc.nverts >= 0xFFFFFFFFull || nstream >= 0x3FFFFFFFull) return EUC_ERR_INVALID;
     SceneDev &s = p.d;
     s.verts = (const uint8_t *)sc.vertices;
     s.idx = sc.indices;
@@ -233,8 +233,19 @@ int plan_scene(const euc_scene &sc, Plan &p) {
     s.nverts = sc.nverts;
     s.nstream = nstream;
     s.lay = l;
-    s.ntris = (uint32_t)(nstream / 3);
-    s.ngroups = (uint32_t)((nstream + 2) / 3);
+    // primitive slots: one per triangle / line; the index checks of a
+    // trailing partial primitive belong to its slot (primitives.rs:18-104)
+    s.prim = d.primitives;
+    if (d.primitives == EUC_PRIM_TRIANGLE_LIST) {
+        s.ntris = (uint32_t)(nstream / 3);
+        s.ngroups = (uint32_t)((nstream + 2) / 3);
+    } else if (d.primitives == EUC_PRIM_LINE_LIST) {
+        s.ntris = (uint32_t)(nstream / 2);
+        s.ngroups = (uint32_t)((nstream + 1) / 2);
+    } else {  // three lines per complete triangle
+        s.ntris = (uint32_t)(3 * (nstream / 3));
+        s.ngroups = (uint32_t)(3 * ((nstream + 2) / 3));
+    }
     s.W = W;
     s.H = H;
     s.gr = (uint32_t)gr;
@@ -548,10 +559,11 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
     const unsigned rgrid = (unsigned)(ctx->nsm * (tu.raster_blocks_per_sm ? (int)tu.raster_blocks_per_sm
                                                                            : ctx->raster_blocks));
     const int witems = tu.raster_warp_rows ? (int)tu.raster_warp_rows : kWarpItems;
+    const bool probe = tu.raster_probe == 1;
     k_raster<<<rgrid, kBlock, 0, st>>>(dsc, (const TriRec *)ctx->recs.p, (const uint32_t *)ctx->live_tri.p,
                                        (const uint64_t *)ctx->live_rowoff.p, (unsigned long long *)ctx->totals.p,
                                        (const int *)ctx->err.p, (unsigned long long *)ctx->vbuf.p,
-                                       (SceneStats *)ctx->stats.p, 0, nullptr, witems);
+                                       (SceneStats *)ctx->stats.p, 0, nullptr, witems, probe);
     ctx->launches += 5;
     // ordered scenes: scan the per-pixel counts, size the fragment buffer
     // (one stream synchronisation), fill the lists in a second raster pass
@@ -574,7 +586,7 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
         k_raster<<<rgrid, kBlock, 0, st>>>(dsc, (const TriRec *)ctx->recs.p, (const uint32_t *)ctx->live_tri.p,
                                            (const uint64_t *)ctx->live_rowoff.p, (unsigned long long *)ctx->totals.p,
                                            (const int *)ctx->err.p, (unsigned long long *)ctx->vbuf.p,
-                                           (SceneStats *)ctx->stats.p, 1, (uint2 *)ctx->frags.p, witems);
+                                           (SceneStats *)ctx->stats.p, 1, (uint2 *)ctx->frags.p, witems, probe);
         ctx->launches += 3;
     }
     cudaEvent_t e5 = prof_event(ctx, st);
@@ -697,7 +709,8 @@ int euc_ctx_set_tuning(euc_ctx *ctx, const euc_tuning *t) {
         v = *t;
         if (v.raster_warp_rows && (v.raster_warp_rows % 32 || v.raster_warp_rows > (uint32_t)kWarpItems))
             return EUC_ERR_INVALID;
-        if (v.raster_blocks_per_sm > 64 || v.chunk_group > 1024 || v.chunk_blocks_per_sm > 64) return EUC_ERR_INVALID;
+        if (v.raster_blocks_per_sm > 64 || v.chunk_group > 1024 || v.chunk_blocks_per_sm > 64 || v.raster_probe > 2)
+            return EUC_ERR_INVALID;
     }
     std::lock_guard<std::mutex> g(ctx->mu);
     ctx->tune = v;
@@ -907,6 +920,62 @@ int euc_graph_destroy(euc_graph *g) {
     cudaSetDevice(g->ctx->device);
     cudaDeviceSynchronize();
     graph_free(g);
+    return EUC_OK;
+}
+
+int euc_texture_ingest(euc_ctx *ctx, const void *src, uint32_t width, uint32_t height, uint64_t src_pitch,
+                       uint32_t src_format, void *dst, uint64_t dst_pitch, void *stream) {
+    if (!ctx || !src || !dst || width < 1 || height < 1 || src_format > EUC_SRC_R32F) return EUC_ERR_INVALID;
+    const uint32_t sbpp = src_bpp(src_format);
+    const uint64_t srow = (uint64_t)width * sbpp, drow = (uint64_t)width * 4;
+    if (!src_pitch) src_pitch = srow;
+    if (!dst_pitch) dst_pitch = drow;
+    if (src_pitch < srow || dst_pitch < drow || (dst_pitch & 3) || ((uintptr_t)dst & 3)) return EUC_ERR_INVALID;
+    if (src_format == EUC_SRC_R32F && ((src_pitch & 3) || ((uintptr_t)src & 3))) return EUC_ERR_INVALID;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CUDA_TRY(cudaSetDevice(ctx->device));
+    const cudaStream_t st = (cudaStream_t)stream;
+    cudaPointerAttributes attr{};
+    const bool on_device = cudaPointerGetAttributes(&attr, src) == cudaSuccess &&
+                           (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged);
+    (void)cudaGetLastError();
+    const uint8_t *from = (const uint8_t *)src;
+    uint64_t pitch = src_pitch;
+    if (!on_device) {  // stage the rows, packed, through the context
+        int rc;
+        if ((rc = grow(ctx->h_tex[0], srow * height))) return rc;
+        CUDA_TRY(cudaMemcpy2DAsync(ctx->h_tex[0].p, srow, src, src_pitch, srow, height, cudaMemcpyHostToDevice, st));
+        from = (const uint8_t *)ctx->h_tex[0].p;
+        pitch = srow;
+    }
+    const dim3 grid((unsigned)((width + 31) / 32), (unsigned)std::min<uint32_t>(height, 65535u));
+    k_ingest<<<grid, dim3(32, 8), 0, st>>>(from, pitch, src_format, (uint8_t *)dst, dst_pitch, width, height);
+    ctx->launches += 1;
+    CUDA_TRY(cudaGetLastError());
+    if (!on_device) CUDA_TRY(cudaStreamSynchronize(st));  // the staging is reused by the next call
+    return EUC_OK;
+}
+
+int euc_sample_nearest(const void *texels, uint32_t ndim, const uint32_t *size, uint32_t texel_bytes, uint32_t wrap,
+                       const float *queries, uint64_t count, void *out, void *stream) {
+    if (!size || ndim < 1 || ndim > 4 || texel_bytes < 1 || texel_bytes > 16 || wrap > EUC_WRAP_MIRROR)
+        return EUC_ERR_INVALID;
+    uint32_t sz[4] = {1, 1, 1, 1};
+    for (uint32_t a = 0; a < ndim; ++a) {
+        if (size[a] < 1) return EUC_ERR_INVALID;  // Denormalize's `scale - 1` underflows on an empty axis
+        sz[a] = size[a];
+    }
+    if (!count) return EUC_OK;
+    if (!texels || !queries || !out) return EUC_ERR_INVALID;
+    const cudaStream_t st = (cudaStream_t)stream;
+    int nsm = 0, dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const uint64_t blocks = std::min<uint64_t>((count + kBlock - 1) / kBlock, (uint64_t)nsm * 16);
+    k_sample_nearest<<<(unsigned)blocks, kBlock, 0, st>>>((const uint8_t *)texels, ndim,
+                                                          make_uint4(sz[0], sz[1], sz[2], sz[3]), texel_bytes, wrap,
+                                                          queries, count, (uint8_t *)out);
+    CUDA_TRY(cudaGetLastError());
     return EUC_OK;
 }
 
@@ -1189,7 +1258,7 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
     k_raster<<<(unsigned)(nsm * raster_blocks_per_sm()), kBlock, 0, st>>>(
         dsc, (const TriRec *)(a + kNaOffRecs), (const uint32_t *)(a + kNaOffLiveTri), (const uint64_t *)(a + kNaOffLiveOff),
         (unsigned long long *)(a + kNaOffTotals), (const int *)(a + kNaOffErr),
-        (unsigned long long *)(a + kNaOffVbuf), (SceneStats *)(a + kNaOffStats), 0, nullptr, kWarpItems);
+        (unsigned long long *)(a + kNaOffVbuf), (SceneStats *)(a + kNaOffStats), 0, nullptr, kWarpItems, false);
     na_dispatch(false, d.shader, dsc, rbase, resolve_blocks(d), a, st);
     if (device_status)
         CUDA_TRY(cudaMemcpyAsync(device_status, a + kNaOffErr, sizeof(int), cudaMemcpyDeviceToDevice, st));

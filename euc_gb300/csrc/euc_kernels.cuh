@@ -57,13 +57,13 @@ struct SceneDev {
     uint64_t tri_base;        // first primitive record (multiple of kBlock)
     uint64_t pix_base;        // first visibility key (multiple of kBlock)
     euc_vertex_layout lay;
-    uint32_t ntris;           // complete primitives
-    uint32_t ngroups;         // ceil(nstream / 3): groups whose indices are checked
+    uint32_t ntris;           // complete primitives (triangles or lines)
+    uint32_t ngroups;         // primitive slots whose indices are checked (partial one included)
     uint32_t W, H, gr, level;
     uint32_t ppitch, dpitch, pfmt;
     uint32_t pixel_write, depth_test, depth_write, yflip, zclip, cull, blend, keytype;
     float zmin, zmax;
-    uint32_t shader, pad0;
+    uint32_t shader, prim;    // enum euc_shader, enum euc_primitives
 };
 
 // Per-primitive record written by k_setup (128 bytes, 16-byte aligned).
@@ -179,6 +179,147 @@ __global__ void __launch_bounds__(kBlock) k_vertex(const SceneDev *__restrict__ 
 }
 
 // ---------------------------------------------------------------------------
+// Lines (lines.rs:30-119).  A line record reuses TriRec's storage:
+//   o = {screen x0, screen y0, norm}, zc = {euclidean z0, z1},
+//   ln = {major start a1, minor start b1, |dmajor|, |dminor|, first step},
+//   bx0 / bx1 = the window's minor-axis range (inclusive), by0 = 0,
+//   by1 = steps in the window's major range, v = {vertex 0, vertex 1},
+//   flags: kLineUseX (frac along x), kLineXMajor, kLineNegMaj, kLineNegMin.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kLineUseX = 4u, kLineXMajor = 8u, kLineNegMaj = 16u, kLineNegMin = 32u;
+
+// `f as isize` (saturating, NaN -> 0).
+EUC_DEV long long as_isize(float v) {
+    if (isnan(v)) return 0;
+    if (v >= 9.2233720368547758e18f) return 0x7FFFFFFFFFFFFFFFll;
+    if (v <= -9.2233720368547758e18f) return (long long)0x8000000000000000ull;
+    return (long long)v;
+}
+// f32::clamp with ordered bounds (a NaN stays NaN).
+EUC_DEV float fclamp(float v, float lo, float hi) { return v < lo ? lo : (v > hi ? hi : v); }
+// isize subtraction / abs with wrapping (euc builds without overflow checks).
+EUC_DEV long long wsub(long long a, long long b) { return (long long)((unsigned long long)a - (unsigned long long)b); }
+EUC_DEV long long wabs(long long a) { return a < 0 ? (long long)(0ull - (unsigned long long)a) : a; }
+
+// Setup of line slot lt.  The pixels are clipline's: the Bresenham line
+// between the truncated end points, both ends included, inside the window
+// (x in [wx1, wx2), y in [wy1, wy2)) -- see the oracle's bresenham_clipped
+// for the restatement and why the band clamp of the window does not change
+// the pixel set.  Lines with a coordinate beyond 2^30 draw nothing.
+EUC_DEV void setup_line(const SceneDev &s, int si, uint64_t lt, uint64_t t, const float4 *__restrict__ clip,
+                        TriRec *__restrict__ recs, int *__restrict__ err, uint32_t &nrows, uint32_t &cx0,
+                        uint32_t &cy0, uint32_t &cx1, uint32_t &cy1) {
+    uint64_t e[2];
+    bool ok = true;
+    if (s.prim == EUC_PRIM_LINE_LIST) {
+        e[0] = 2 * lt;
+        e[1] = 2 * lt + 1;
+    } else {
+        const uint64_t j = lt / 3, k = lt % 3;
+        e[0] = 3 * j + k;
+        e[1] = 3 * j + (k + 1) % 3;
+        if (k == 0)  // the first edge checks the whole group of three
+            for (uint64_t q = 3 * j; q < 3 * j + 3 && q < s.nstream; ++q) {
+                const uint64_t id = s.idx ? (uint64_t)__ldg(s.idx + q) : q;
+                if (id >= s.nverts) ok = false;  // index.rs:53
+            }
+    }
+    uint32_t vid[2] = {0, 0};
+    bool mine = true;  // both end indices valid, so their clip positions may be read
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        if (e[k] < s.nstream) {
+            const uint64_t id = s.idx ? (uint64_t)__ldg(s.idx + e[k]) : e[k];
+            if (id >= s.nverts) {
+                ok = false;
+                mine = false;
+            }
+            vid[k] = (uint32_t)id;
+        } else {
+            mine = false;
+        }
+    }
+    if (!ok) atomicCAS(err + si, 0, EUC_ERR_INDEX_OOB);
+    if (!ok || !mine || lt >= s.ntris) return;
+    const float flip1 = s.yflip ? -1.0f : 1.0f;
+    const float size_x = (float)s.W, size_y = (float)s.H;
+    float ez[2], sx[2], sy[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const float4 c = clip[s.vtx_base + vid[k]];
+        const float w = rmax(c.w, 0.0001f);  // lines.rs:45-48
+        const float ex = (c.x * 1.0f) / w, ey = (c.y * flip1) / w;
+        ez[k] = c.z / w;
+        sx[k] = size_x * (ex * 0.5f + 0.5f);  // lines.rs:53-55
+        sy[k] = size_y * (ey * -0.5f + 0.5f);
+    }
+    const long long x1 = as_isize(sx[0]), y1 = as_isize(sy[0]), x2 = as_isize(sx[1]), y2 = as_isize(sy[1]);
+    const long long wx1 = as_isize(fclamp(rmin(sx[0], sx[1]) + 0.0f, 0.0f, size_x));
+    const long long wy1 = as_isize(fclamp(rmin(sy[0], sy[1]) + 0.0f, 0.0f, size_y));
+    const long long wx2 = as_isize(fclamp(rmax(sx[0], sx[1]) + 1.0f, 0.0f, size_x));
+    const long long wy2 = as_isize(fclamp(rmax(sy[0], sy[1]) + 1.0f, 0.0f, size_y));
+    const bool use_x = wabs(wsub(x1, x2)) > wabs(wsub(y1, y2));  // lines.rs:73
+    const float norm = 1.0f / (use_x ? sx[1] - sx[0] : sy[1] - sy[0]);
+    const long long lim = 1ll << 30;
+    if (wx2 <= wx1 || wy2 <= wy1) return;  // empty window
+    if (x1 <= -lim || x1 >= lim || x2 <= -lim || x2 >= lim || y1 <= -lim || y1 >= lim || y2 <= -lim || y2 >= lim)
+        return;
+    const long long dx = x2 - x1, dy = y2 - y1;
+    const bool xmaj = (dx < 0 ? -dx : dx) >= (dy < 0 ? -dy : dy);
+    const long long a1 = xmaj ? x1 : y1, b1 = xmaj ? y1 : x1;
+    const long long dmaj = xmaj ? dx : dy, dmin = xmaj ? dy : dx;
+    const long long amaj = dmaj < 0 ? -dmaj : dmaj, amin = dmin < 0 ? -dmin : dmin;
+    const long long wa1 = xmaj ? wx1 : wy1, wa2 = (xmaj ? wx2 : wy2) - 1;
+    const long long wb1 = xmaj ? wy1 : wx1, wb2 = (xmaj ? wy2 : wx2) - 1;
+    long long i_lo, i_hi;
+    if (dmaj >= 0) {
+        i_lo = wa1 - a1;
+        i_hi = wa2 - a1;
+    } else {
+        i_lo = a1 - wa2;
+        i_hi = a1 - wa1;
+    }
+    if (i_lo < 0) i_lo = 0;
+    if (i_hi > amaj) i_hi = amaj;
+    if (i_hi < i_lo) return;
+    TriRec r;
+    r.o[0] = sx[0];
+    r.o[1] = sy[0];
+    r.o[2] = norm;
+    r.zc[0] = ez[0];
+    r.zc[1] = ez[1];
+    r.zc[2] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r.dx[k] = r.dy[k] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) r.vby[k] = 0.0f;
+    r.pad[0] = (uint32_t)(int32_t)a1;
+    r.pad[1] = (uint32_t)(int32_t)b1;
+    r.pad[2] = (uint32_t)amaj;
+    r.pad[3] = (uint32_t)amin;
+    r.pad[4] = (uint32_t)i_lo;
+    r.bx0 = (uint32_t)wb1;
+    r.bx1 = (uint32_t)wb2;
+    r.by0 = 0;
+    r.by1 = (uint32_t)(i_hi - i_lo + 1);
+    r.v[0] = vid[0];
+    r.v[1] = vid[1];
+    r.v[2] = vid[1];
+    r.scene = (uint32_t)si;
+    r.flags = (use_x ? kLineUseX : 0u) | (xmaj ? kLineXMajor : 0u) | (dmaj < 0 ? kLineNegMaj : 0u) |
+              (dmin < 0 ? kLineNegMin : 0u);
+    const float4 *src = reinterpret_cast<const float4 *>(&r);
+    float4 *dst = reinterpret_cast<float4 *>(recs + t);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) dst[k] = src[k];
+    nrows = r.by1;
+    cx0 = (uint32_t)wx1;
+    cx1 = (uint32_t)wx2;
+    cy0 = (uint32_t)wy1;
+    cy1 = (uint32_t)wy2;
+}
+
+// ---------------------------------------------------------------------------
 // k_setup: triangles.rs:55-199, once per primitive (euc repeats it per band;
 // only the bbox clamp depends on the band and that is applied per row).
 // ---------------------------------------------------------------------------
@@ -198,7 +339,9 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
     uint32_t nrows = 0, culled = 0;
     // pixels this primitive may touch: x in [cx0, cx1), y in [cy0, cy1)
     uint32_t cx0 = 0xFFFFFFFFu, cy0 = 0xFFFFFFFFu, cx1 = 0, cy1 = 0;
-    if (lt < s.ngroups) {
+    if (s.prim != EUC_PRIM_TRIANGLE_LIST) {  // uniform: a block holds one scene
+        if (lt < s.ngroups) setup_line(s, si, lt, t, clip, recs, err, nrows, cx0, cy0, cx1, cy1);
+    } else if (lt < s.ngroups) {
         uint32_t vid[3] = {0, 0, 0};
         bool ok = true;
 #pragma unroll
@@ -320,7 +463,13 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
                 r.bx0 = bx0; r.bx1 = bx1; r.by0 = by0; r.by1 = by1;
                 r.v[0] = vid[0]; r.v[1] = vid[1]; r.v[2] = vid[2];
                 r.scene = (uint32_t)si;
-                r.flags = noclip ? 1u : 0u;
+                // bit 1: every row lies in one render_par band and the bbox
+                // extent is below 128, so every row spans the whole bbox
+                // (triangles.rs:224-226) and k_raster skips the band and edge
+                // arithmetic
+                const bool one_band = by1 > by0 && by0 / s.gr == (by1 - 1) / s.gr;
+                const bool full_rows = one_band && (unsigned long long)(bx1 - bx0) * (by1 - by0) < 128ull;
+                r.flags = (noclip ? 1u : 0u) | (full_rows ? 2u : 0u);
 #pragma unroll
                 for (int k = 0; k < 5; ++k) r.pad[k] = 0;
                 const float4 *src = reinterpret_cast<const float4 *>(&r);
@@ -443,9 +592,10 @@ __host__ __device__ inline uint64_t rect_area(const uint4 &c) {
 // is spent on pixels that no primitive reaches.
 constexpr int kChunkGroup = 16;
 
-// Each thread of k_init initialises kInitPer entries of the covered rectangle
-// (their depth loads are in flight together); a chunk is kBlock * kInitPer
-// entries.
+// Each thread of k_init initialises kInitPer entries of the covered rectangle,
+// kBlock apart, so that every load and store instruction of a warp covers 32
+// consecutive entries and the kInitPer depth loads are in flight together; a
+// chunk is kBlock * kInitPer entries.
 constexpr int kInitPer = 4;
 constexpr int kInitChunk = kBlock * kInitPer;
 
@@ -470,39 +620,34 @@ __global__ void __launch_bounds__(kBlock) k_init(const SceneDev *__restrict__ sc
         for (uint64_t c = c0; c < c0 + group && c < nchunks; ++c) {
             si = advance_scene(ibase, nsc, si, c);
             const SceneDev &s = sc[si];
-            const uint64_t i0 = (c - ibase[si]) * kInitChunk + (uint64_t)threadIdx.x * kInitPer;
+            // pixel and entry indices within a scene fit 32 bits (plan_scene)
+            const uint32_t i0 = (uint32_t)(c - ibase[si]) * kInitChunk + threadIdx.x;
             unsigned long long *row0 = vbuf + s.pix_base;
             if (s.keytype == KEY_ORDERED) {
                 // every entry, padding included (the pixel scan sums them all):
                 // no fragment yet, cursor 0
-                const uint64_t lim = ((uint64_t)s.W * s.H + kBlock - 1) / kBlock * kBlock;
-                if (i0 < lim) {  // lim and i0 are multiples of kInitPer
-                    reinterpret_cast<ulonglong2 *>(row0 + i0)[0] = make_ulonglong2(0ull, 0ull);
-                    reinterpret_cast<ulonglong2 *>(row0 + i0)[1] = make_ulonglong2(0ull, 0ull);
-                }
+                const uint32_t lim = (s.W * s.H + kBlock - 1) / kBlock * kBlock;
+#pragma unroll
+                for (int k = 0; k < kInitPer; ++k)
+                    if (i0 + k * kBlock < lim) row0[i0 + k * kBlock] = 0ull;
                 continue;
             }
-            // entries i0 .. i0+3 of the covered rectangle, row by row
+            // entries i0, i0 + kBlock, ... of the covered rectangle, row by row
             const uint4 cv = cov[si];
-            const uint64_t area = rect_area(cv);
+            const uint32_t area = (uint32_t)rect_area(cv);
             if (i0 >= area) continue;
             const uint32_t rw = ~cv.z - cv.x;
-            uint32_t y = (uint32_t)(i0 / rw);
-            uint32_t x = cv.x + (uint32_t)(i0 - (uint64_t)y * rw);
-            y += cv.y;
             uint32_t px[kInitPer];
             float d[kInitPer];
 #pragma unroll
             for (int k = 0; k < kInitPer; ++k) {
-                const bool live = i0 + k < area;
-                px[k] = live ? y * s.W + x : 0xFFFFFFFFu;  // pixel indices fit 32 bits (plan_scene)
+                const uint32_t i = i0 + k * kBlock;
+                const bool live = i < area;
+                const uint32_t ry = i / rw, x = cv.x + (i - ry * rw), y = cv.y + ry;
+                px[k] = live ? y * s.W + x : 0xFFFFFFFFu;
                 d[k] = (live && s.keytype == KEY_MIN)
                            ? *reinterpret_cast<const float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x)
                            : 0.0f;
-                if (++x == ~cv.z) {
-                    x = cv.x;
-                    ++y;
-                }
             }
 #pragma unroll
             for (int k = 0; k < kInitPer; ++k)
@@ -515,19 +660,77 @@ __global__ void __launch_bounds__(kBlock) k_init(const SceneDev *__restrict__ sc
 // ---------------------------------------------------------------------------
 // k_raster: one (primitive, row) at a time per thread, warp-scheduled.
 // ---------------------------------------------------------------------------
+// Step k (in the window's major range) of line t: its pixel, then the same
+// candidate handling as a triangle's pixel (lines.rs:79-97).
+EUC_DEV void raster_line_step(const SceneDev &s, const TriRec &r, uint32_t t, uint32_t k,
+                              unsigned long long *__restrict__ vbuf, uint32_t &cnt, int phase,
+                              uint2 *__restrict__ frags, bool probe) {
+    const uint64_t i = (uint64_t)r.pad[4] + k;
+    const uint64_t amaj = r.pad[2], amin = r.pad[3];
+    // |dmajor|, |dminor| < 2^31: the numerator stays below 2^64
+    const uint64_t m = amaj ? (2 * amin * i + amaj - 1) / (2 * amaj) : 0;
+    const long long a = (long long)(int32_t)r.pad[0] + ((r.flags & kLineNegMaj) ? -(long long)i : (long long)i);
+    const long long b = (long long)(int32_t)r.pad[1] + ((r.flags & kLineNegMin) ? -(long long)m : (long long)m);
+    if (b < (long long)r.bx0 || b > (long long)r.bx1) return;  // outside the window's minor range
+    const uint32_t x = (uint32_t)((r.flags & kLineXMajor) ? a : b), y = (uint32_t)((r.flags & kLineXMajor) ? b : a);
+    const float frac = ((r.flags & kLineUseX) ? (float)x - r.o[0] : (float)y - r.o[1]) * r.o[2];
+    const float z = r.zc[0] + frac * (r.zc[1] - r.zc[0]);
+    if (s.zclip && !(s.zmin <= z && z <= s.zmax)) return;  // CoordinateMode::passes_z_clip
+    unsigned long long *key = vbuf + s.pix_base + (uint64_t)y * s.W + x;
+    if (s.keytype == KEY_ORDERED) {
+        unsigned int *e = reinterpret_cast<unsigned int *>(key);
+        if (phase == 0) {
+            ++cnt;
+            atomicAdd(e, 1u);
+        } else {
+            const unsigned int slot = __ldcg(e) + atomicAdd(e + 1, 1u);
+            frags[slot] = make_uint2(t, __float_as_uint(z));
+        }
+        return;
+    }
+    ++cnt;
+    bool pass;
+    unsigned long long kv;
+    if (s.keytype == KEY_MIN) {
+        pass = !isnan(z);
+        const float zc = z == 0.0f ? 0.0f : z;
+        const uint32_t o = s.depth_test == EUC_TEST_GREATER ? ~ord_f32(zc) : ord_f32(zc);
+        kv = ((unsigned long long)o << 32) | (((t + 1u) << 1) | ((z == 0.0f && signbit(z)) ? 1u : 0u));
+    } else {
+        pass = true;
+        if (s.depth_test != EUC_TEST_NONE) {
+            const float old = *reinterpret_cast<const float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x);
+            if (s.depth_test == EUC_TEST_LESS) pass = z < old;
+            else if (s.depth_test == EUC_TEST_EQUAL) pass = z == old;
+            else pass = z > old;
+        }
+        kv = ((unsigned long long)(~t) << 32) | __float_as_uint(z);
+    }
+    if (!pass) return;
+    if (!probe || kv < __ldcg(key)) atomicMin(key, kv);
+}
+
 EUC_DEV void raster_row(const SceneDev &s, const TriRec &r, uint32_t t, uint32_t y,
-                        unsigned long long *__restrict__ vbuf, uint32_t &cnt, int phase, uint2 *__restrict__ frags) {
-    // band of this row and the band-clamped bbox (pipeline.rs:341-360, triangles.rs:114-139)
-    const uint32_t lo = (y / s.gr) * s.gr;
-    const uint32_t hi = min(lo + s.gr, s.H);
-    const uint32_t by0c = max(r.by0, lo), by1c = min(r.by1, hi);
-    const unsigned long long ext = (unsigned long long)(r.bx1 - r.bx0) * (unsigned long long)(by1c - by0c);
+                        unsigned long long *__restrict__ vbuf, uint32_t &cnt, int phase, uint2 *__restrict__ frags,
+                        bool probe) {
+    if (s.prim != EUC_PRIM_TRIANGLE_LIST) {  // lines: `y` is the step within the window
+        raster_line_step(s, r, t, y, vbuf, cnt, phase, frags, probe);
+        return;
+    }
     const float yf = (float)y;
     uint32_t xs, xe;
-    if (ext < 128ull) {  // triangles.rs:224-226
+    bool full = r.flags & 2u;  // one band, extent < 128 (k_setup)
+    if (!full) {
+        // band of this row and the band-clamped bbox (pipeline.rs:341-360, triangles.rs:114-139)
+        const uint32_t lo = (y / s.gr) * s.gr;
+        const uint32_t hi = min(lo + s.gr, s.H);
+        const uint32_t by0c = max(r.by0, lo), by1c = min(r.by1, hi);
+        full = (unsigned long long)(r.bx1 - r.bx0) * (unsigned long long)(by1c - by0c) < 128ull;
+    }
+    if (full) {  // triangles.rs:224-226
         xs = r.bx0;
         xe = r.bx1;
-    } else {             // triangles.rs:228-253
+    } else {     // triangles.rs:228-253
         const float ax = r.vby[0], ay = r.vby[1], bxv = r.vby[2], byv = r.vby[3], cx = r.vby[4], cy = r.vby[5];
         const float ac = ax + ((yf - ay) / (cy - ay)) * (cx - ax);
         float lo_f, hi_f;
@@ -563,6 +766,7 @@ EUC_DEV void raster_row(const SceneDev &s, const TriRec &r, uint32_t t, uint32_t
     // are gathered kWalk at a time so that their key loads are in flight
     // together instead of one L2 round trip per pixel.
     constexpr int kWalk = 4;
+    static_assert(kWalk == 4, "the empty-group test below names four candidates");
     for (uint32_t x = xs; x < xe; x += kWalk) {
         float zz[kWalk];
         bool cand[kWalk];
@@ -584,6 +788,9 @@ EUC_DEV void raster_row(const SceneDev &s, const TriRec &r, uint32_t t, uint32_t
                 w2 = w2 + d2;
             }
         }
+        // most groups of a full-bbox row (extent < 128) hold no candidate:
+        // only the weight additions above are needed there
+        if (!(cand[0] | cand[1] | cand[2] | cand[3])) continue;
         if (s.keytype == KEY_ORDERED) {
             // phase 0 counts each pixel's candidates (low word of its entry);
             // phase 1 appends (primitive, z) at offset (low word, set by the
@@ -628,12 +835,21 @@ EUC_DEV void raster_row(const SceneDev &s, const TriRec &r, uint32_t t, uint32_t
                 key[k] = tlast | __float_as_uint(z);
             }
         }
-        unsigned long long cur[kWalk];
+        if (probe) {
+            // read the keys first and skip the atomics that cannot win (high
+            // depth complexity: most candidates lose)
+            unsigned long long cur[kWalk];
 #pragma unroll
-        for (int k = 0; k < kWalk; ++k) cur[k] = pass[k] ? __ldcg(row_keys + x + k) : 0ull;
+            for (int k = 0; k < kWalk; ++k) cur[k] = pass[k] ? __ldcg(row_keys + x + k) : 0ull;
 #pragma unroll
-        for (int k = 0; k < kWalk; ++k)
-            if (pass[k] && key[k] < cur[k]) atomicMin(row_keys + x + k, key[k]);
+            for (int k = 0; k < kWalk; ++k)
+                if (pass[k] && key[k] < cur[k]) atomicMin(row_keys + x + k, key[k]);
+        } else {
+            // fire-and-forget reductions: the walk never waits on memory
+#pragma unroll
+            for (int k = 0; k < kWalk; ++k)
+                if (pass[k]) atomicMin(row_keys + x + k, key[k]);
+        }
     }
 }
 
@@ -653,7 +869,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_raster(const SceneDev *__restrict
                                                    unsigned long long *__restrict__ totals,
                                                    const int *__restrict__ err, unsigned long long *__restrict__ vbuf,
                                                    SceneStats *__restrict__ stats, int phase,
-                                                   uint2 *__restrict__ frags, int witems) {
+                                                   uint2 *__restrict__ frags, int witems, bool probe) {
     __shared__ uint64_t s_off[kBlock / 32][kWarpItems];
     const int lane = threadIdx.x & 31;
     uint64_t *off = s_off[threadIdx.x >> 5];
@@ -671,8 +887,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_raster(const SceneDev *__restrict
         uint64_t lo = 0, hi = nlive;
         while (hi - lo > 32) {
             const uint64_t step = (hi - lo + 31) / 32;
-            const uint64_t probe = lo + lane * step;
-            const bool le = probe < hi && live_rowoff[probe] <= base;
+            const uint64_t at = lo + lane * step;
+            const bool le = at < hi && live_rowoff[at] <= base;
             const int k = 31 - __clz(__ballot_sync(0xFFFFFFFFu, le));  // lane 0 always qualifies
             lo = lo + (uint64_t)k * step;
             hi = min(lo + step, hi);
@@ -699,7 +915,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_raster(const SceneDev *__restrict
             if (err[scene]) continue;
             if (phase == 1 && sc[scene].keytype != KEY_ORDERED) continue;  // the fill pass is for ordered scenes
             uint32_t cnt = 0;
-            raster_row(sc[scene], r, t, r.by0 + (uint32_t)(i - off[a]), vbuf, cnt, phase, frags);
+            raster_row(sc[scene], r, t, r.by0 + (uint32_t)(i - off[a]), vbuf, cnt, phase, frags, probe);
             if (scene0 == 0xFFFFFFFFu) scene0 = scene;
             if (scene == scene0) cnt0 += cnt;
             else if (cnt) atomicAdd(&stats[scene].candidates, (unsigned long long)cnt);
@@ -730,6 +946,21 @@ EUC_DEV void get_v_data(const TriRec &r, const float *__restrict__ vd0, const fl
     const float p0 = w[0] * rr, p1 = w[1] * rr, p2 = wu2 * rr;
 #pragma unroll
     for (int i = 0; i < F::NV; ++i) out[i] = (vd0[i] * p0 + vd1[i] * p1) + vd2[i] * p2;
+}
+
+// The winner's vertex outputs at (xf, yf): get_v_data for a triangle,
+// weighted_sum2 of the two ends for a line (lines.rs:98-110).
+template <class F>
+EUC_DEV void vdata_at(const SceneDev &s, const TriRec &r, const float *__restrict__ vb, float xf, float yf,
+                      float *out) {
+    const float *v0 = vb + (uint64_t)r.v[0] * F::NV, *v1 = vb + (uint64_t)r.v[1] * F::NV;
+    if (s.prim != EUC_PRIM_TRIANGLE_LIST) {
+        const float frac = ((r.flags & kLineUseX) ? xf - r.o[0] : yf - r.o[1]) * r.o[2];
+#pragma unroll
+        for (int i = 0; i < F::NV; ++i) out[i] = v0[i] * (1.0f - frac) + v1[i] * frac;
+        return;
+    }
+    get_v_data<F>(r, v0, v1, vb + (uint64_t)r.v[2] * F::NV, xf, yf, out);
 }
 
 // Decodes a visibility key; false when no fragment passed at this pixel.
@@ -779,12 +1010,29 @@ __host__ __device__ inline bool resolve_by_quads(const SceneDev &s) {
     return s.level == 1 && s.pixel_write && s.keytype != KEY_ORDERED;
 }
 
+// Shaders cheap enough to be evaluated where their pixel is (no job list).
+constexpr uint32_t kDirectShaders = (FlatFn::kDirect ? 1u << EUC_SHADER_FLAT : 0u) |
+                                    (VColorFn::kDirect ? 1u << EUC_SHADER_VCOLOR : 0u) |
+                                    (GouraudFn::kDirect ? 1u << EUC_SHADER_GOURAUD : 0u) |
+                                    (TexturedFn::kDirect ? 1u << EUC_SHADER_TEXTURED : 0u) |
+                                    (PhongFn::kDirect ? 1u << EUC_SHADER_PHONG : 0u) |
+                                    (ShadowFn::kDirect ? 1u << EUC_SHADER_SHADOW : 0u);
+
+// Scenes resolved kDirectPer pixels per thread with no shared memory: depth
+// only, or a cheap shader without MSAA.
+constexpr int kDirectPer = 4;
+__host__ __device__ inline bool resolve_direct(const SceneDev &s) {
+    return s.keytype != KEY_ORDERED &&
+           (!s.pixel_write || (s.level == 0 && ((kDirectShaders >> s.shader) & 1u)));
+}
+
 // k_resolve chunks (blocks of work) of a scene: kBlock pixels of the covered
 // rectangle, or kBlock/32 warp tiles of 16x2 pixels over the row pairs and
 // 16-pixel columns that meet it.
 __host__ __device__ inline uint64_t resolve_chunks(const SceneDev &s, const uint4 &cv) {
     const uint64_t area = rect_area(cv);
     if (area == 0) return 0;
+    if (resolve_direct(s)) return (area + kBlock * kDirectPer - 1) / (kBlock * kDirectPer);
     if (resolve_by_quads(s)) {
         const uint64_t pairs = pair_of_row(~cv.w - 1, s.gr) - pair_of_row(cv.y, s.gr) + 1;
         const uint64_t cols = ((~cv.z - 1) >> 4) - (cv.x >> 4) + 1;
@@ -850,6 +1098,44 @@ struct ResolveSmem {
     uint32_t scan[kBlock / 32 + 1];
 };
 
+// Chunk `lb` of a resolve_direct scene: kBlock * kDirectPer pixels of the
+// covered rectangle, each thread taking kDirectPer of them kBlock apart (the
+// key loads of a thread are in flight together).
+template <class F>
+EUC_DEV void resolve_direct_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, const TriRec *__restrict__ recs,
+                                  const float *__restrict__ vdata, const unsigned long long *__restrict__ vbuf) {
+    const uint32_t rw = ~cv.z - cv.x, area = (uint32_t)rect_area(cv);  // pixel indices fit 32 bits
+    const uint32_t i0 = (uint32_t)lb * (kBlock * kDirectPer) + threadIdx.x;
+    uint32_t px[kDirectPer], py[kDirectPer];
+    unsigned long long key[kDirectPer];
+#pragma unroll
+    for (int k = 0; k < kDirectPer; ++k) {
+        const uint32_t i = i0 + k * kBlock;
+        const uint32_t ry = i / rw;
+        px[k] = cv.x + (i - ry * rw);
+        py[k] = i < area ? cv.y + ry : 0xFFFFFFFFu;
+        key[k] = i < area ? vbuf[s.pix_base + (uint64_t)py[k] * s.W + px[k]] : 0ull;
+    }
+#pragma unroll 1
+    for (int k = 0; k < kDirectPer; ++k) {
+        uint32_t t;
+        float z;
+        if (py[k] == 0xFFFFFFFFu || !decode_key(s, key[k], t, z)) continue;
+        const uint32_t x = px[k], y = py[k];
+        if (s.depth_write) *reinterpret_cast<float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x) = z;
+        if (!s.pixel_write) continue;
+        if constexpr (F::kDirect) {
+            const typename F::U &u = *reinterpret_cast<const typename F::U *>(s.uniforms);
+            const float *vb = vdata + s.vd_base;
+            const TriRec &r = recs[t];
+            float vd[F::NV], frag[F::NF];
+            vdata_at<F>(s, r, vb, (float)x, (float)y, vd);
+            F::fragment(u, vd, frag);
+            store_pixel<F>(s, x, y, frag);
+        }
+    }
+}
+
 // One 256-pixel chunk `lb` of scene `s`; every thread of the block calls it.
 template <class F>
 EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, const TriRec *__restrict__ recs,
@@ -878,12 +1164,12 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
         }
     } else {
         const uint32_t rw = ~cv.z - cv.x;
-        const uint64_t i = lb * kBlock + tid;
-        inside = i < rect_area(cv);
+        const uint32_t i = (uint32_t)lb * kBlock + tid;  // pixel indices fit 32 bits (plan_scene)
+        inside = i < (uint32_t)rect_area(cv);
         if (inside) {
-            const uint32_t ry = (uint32_t)(i / rw);
+            const uint32_t ry = i / rw;
             y = cv.y + ry;
-            x = cv.x + (uint32_t)(i - (uint64_t)ry * rw);
+            x = cv.x + (i - ry * rw);
             lo = (y / s.gr) * s.gr;
         }
     }
@@ -892,19 +1178,6 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
     const bool win = inside && decode_key(s, vbuf[s.pix_base + (uint64_t)y * s.W + x], t, z);
     if (win && s.depth_write) *reinterpret_cast<float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x) = z;
     if (!s.pixel_write) return;  // uniform over the block (one scene)
-    if (F::kDirect && s.level == 0) {
-        // a cheap shader without MSAA: each winner is shaded where it is
-        if (!win) return;
-        const typename F::U &u = *reinterpret_cast<const typename F::U *>(s.uniforms);
-        const float *vb = vdata + s.vd_base;
-        const TriRec &r = recs[t];
-        float vd[F::NV], frag[F::NF];
-        get_v_data<F>(r, vb + (uint64_t)r.v[0] * F::NV, vb + (uint64_t)r.v[1] * F::NV, vb + (uint64_t)r.v[2] * F::NV,
-                      (float)x, (float)y, vd);
-        F::fragment(u, vd, frag);
-        store_pixel<F>(s, x, y, frag);
-        return;
-    }
     if (!__syncthreads_or(win)) return;  // nothing to shade in this chunk
 
     // 2. the fragment evaluations this chunk needs, compacted into a job list.
@@ -962,8 +1235,7 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
             yf = (float)(slo + ((((sy - slo) >> L) + (uint32_t)(c >> 1)) << L));
         }
         float vd[F::NV];
-        get_v_data<F>(r, vb + (uint64_t)r.v[0] * F::NV, vb + (uint64_t)r.v[1] * F::NV, vb + (uint64_t)r.v[2] * F::NV,
-                      xf, yf, vd);
+        vdata_at<F>(s, r, vb, xf, yf, vd);
         F::fragment(u, vd, s_frag[slot][c]);
     }
     __syncthreads();
@@ -1014,9 +1286,73 @@ __global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__
         int si = s_scene;
         for (uint64_t c = c0; c < c0 + group && c < c_end; ++c) {
             si = advance_scene(base, n, si, c);
-            resolve_chunk<F>(sc[s_begin + si], cov[s_begin + si], c - base[si], recs, vdata, vbuf, sm);
-            __syncthreads();  // the next chunk reuses shared memory
+            const SceneDev &s = sc[s_begin + si];
+            if (resolve_direct(s)) {  // uniform: one scene per chunk
+                resolve_direct_chunk<F>(s, cov[s_begin + si], c - base[si], recs, vdata, vbuf);
+            } else {
+                resolve_chunk<F>(s, cov[s_begin + si], c - base[si], recs, vdata, vbuf, sm);
+                __syncthreads();  // the next chunk reuses shared memory
+            }
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Texture ingest: one thread per texel, image-crate layouts -> sampler layouts.
+// ---------------------------------------------------------------------------
+__host__ __device__ inline uint32_t src_bpp(uint32_t f) {
+    switch (f) {
+    case EUC_SRC_RGBA8: case EUC_SRC_BGRA8: case EUC_SRC_R32F: return 4;
+    case EUC_SRC_RGB8: return 3;
+    case EUC_SRC_LUMA8: return 1;
+    default: return 2;  // EUC_SRC_LUMA_ALPHA8
+    }
+}
+
+// Block (32, 8): x runs along a row; blocks stride the rows.
+__global__ void __launch_bounds__(256) k_ingest(const uint8_t *__restrict__ src, uint64_t spitch, uint32_t fmt,
+                                                uint8_t *__restrict__ dst, uint64_t dpitch, uint32_t W, uint32_t H) {
+    const uint32_t x = blockIdx.x * 32 + threadIdx.x;
+    if (x >= W) return;
+    const uint32_t bpp = src_bpp(fmt);
+    for (uint32_t y = blockIdx.y * 8 + threadIdx.y; y < H; y += gridDim.y * 8) {
+        const uint8_t *p = src + (uint64_t)y * spitch + (uint64_t)x * bpp;
+        uint32_t *q = reinterpret_cast<uint32_t *>(dst + (uint64_t)y * dpitch) + x;
+        uint32_t r, g, b, a;
+        switch (fmt) {
+        case EUC_SRC_R32F: *q = *reinterpret_cast<const uint32_t *>(p); continue;  // f32 bits as they are
+        case EUC_SRC_RGBA8: r = p[0]; g = p[1]; b = p[2]; a = p[3]; break;
+        case EUC_SRC_BGRA8: r = p[2]; g = p[1]; b = p[0]; a = p[3]; break;
+        case EUC_SRC_RGB8: r = p[0]; g = p[1]; b = p[2]; a = 255; break;
+        case EUC_SRC_LUMA8: r = g = b = p[0]; a = 255; break;
+        default: r = g = b = p[0]; a = p[1]; break;  // luma + alpha
+        }
+        *q = r | (g << 8) | (b << 16) | (a << 24);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// N-dimensional nearest sampling: Nearest::sample (sampler/nearest.rs:27-33)
+// after the wrap of sampler/mod.rs:100-179, Denormalize per axis
+// (math.rs:40-60) and Buffer<T, N>'s linear index (buffer.rs:85-100, axis 0
+// fastest).  One thread per query; texels are copied byte for byte.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_sample_nearest(const uint8_t *__restrict__ tex, uint32_t ndim, uint4 size,
+                                                           uint32_t tb, uint32_t wrap, const float *__restrict__ q,
+                                                           uint64_t count, uint8_t *__restrict__ out) {
+    const uint32_t sz[4] = {size.x, size.y, size.z, size.w};
+    for (uint64_t i = (uint64_t)blockIdx.x * kBlock + threadIdx.x; i < count; i += (uint64_t)gridDim.x * kBlock) {
+        uint64_t lin = 0, factor = 1;
+        for (uint32_t a = 0; a < ndim; ++a) {
+            const float e = wrap_coord(wrap, q[i * ndim + a]);
+            uint32_t idx = sat_u32(rmax(e * (float)sz[a], 0.0f));  // `(e * s as f32).max(0.0) as usize`
+            idx = idx < sz[a] - 1u ? idx : sz[a] - 1u;             // `.min(s - 1)`
+            lin += (uint64_t)idx * factor;
+            factor *= sz[a];
+        }
+        const uint8_t *src = tex + lin * tb;
+        uint8_t *dst = out + i * tb;
+        for (uint32_t b = 0; b < tb; ++b) dst[b] = src[b];
     }
 }
 
@@ -1077,12 +1413,9 @@ __global__ void __launch_bounds__(kBlock) k_oscan_apply(unsigned long long *__re
 template <class F>
 EUC_DEV void shade_at(const SceneDev &s, const typename F::U &u, const TriRec &r, const float *__restrict__ vb,
                       uint32_t x, uint32_t y, float *frag) {
-    const float *v0 = vb + (uint64_t)r.v[0] * F::NV;
-    const float *v1 = vb + (uint64_t)r.v[1] * F::NV;
-    const float *v2 = vb + (uint64_t)r.v[2] * F::NV;
     float vd[F::NV];
     if (s.level == 0) {
-        get_v_data<F>(r, v0, v1, v2, (float)x, (float)y, vd);
+        vdata_at<F>(s, r, vb, (float)x, (float)y, vd);
         F::fragment(u, vd, frag);
         return;
     }
@@ -1093,8 +1426,8 @@ EUC_DEV void shade_at(const SceneDev &s, const typename F::U &u, const TriRec &r
     float t[4][F::NF];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-        get_v_data<F>(r, v0, v1, v2, (float)((px + (uint32_t)(c & 1)) << L),
-                      (float)(lo + ((py + (uint32_t)(c >> 1)) << L)), vd);
+        vdata_at<F>(s, r, vb, (float)((px + (uint32_t)(c & 1)) << L), (float)(lo + ((py + (uint32_t)(c >> 1)) << L)),
+                    vd);
         F::fragment(u, vd, t[c]);
     }
 #pragma unroll

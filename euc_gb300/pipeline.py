@@ -221,7 +221,18 @@ class IndexedVertices:
 
 
 class TriangleList:
-    """The only primitive kind on this path (primitives.rs:21-44)."""
+    """`0 1 2 3 4 5` -> triangles `0 1 2`, `3 4 5` (primitives.rs:18-44)."""
+    KIND = abi.PRIM_TRIANGLE_LIST
+
+
+class LineTriangleList:
+    """Triangles drawn as lines: `0 1 2` -> `0 1`, `1 2`, `2 0` (primitives.rs:46-77)."""
+    KIND = abi.PRIM_LINE_TRIANGLE_LIST
+
+
+class LineList:
+    """`0 1 2 3` -> lines `0 1`, `2 3` (primitives.rs:79-104)."""
+    KIND = abi.PRIM_LINE_LIST
 
 
 # ---------------------------------------------------------------------------
@@ -287,6 +298,7 @@ class Pipeline:
         d.blend = self.BLEND
         d.band_rows = self.band_mode()
         d.flags = 0
+        d.primitives = self.Primitives.KIND
         return d
 
     def render(self, vertices, pixel, depth, ctx=None, stream=None, sync=True):

@@ -135,7 +135,7 @@ class FrameSpec:
 
 def make_desc(shader, pixel_write=1, depth_test=abi.TEST_LESS, depth_write=1, y_axis=abi.Y_DOWN,
               z_clip=(0.0, 1.0), aa_level=0, cull=abi.CULL_BACK, blend=abi.BLEND_REPLACE,
-              band_rows=abi.BANDS_PAR, flags=0, handedness=abi.LEFT):
+              band_rows=abi.BANDS_PAR, flags=0, handedness=abi.LEFT, primitives=abi.PRIM_TRIANGLE_LIST):
     """PipelineDesc with euc's defaults (CoordinateMode::VULKAN, CullMode::Back)."""
     d = abi.PipelineDesc()
     d.shader = shader
@@ -153,6 +153,7 @@ def make_desc(shader, pixel_write=1, depth_test=abi.TEST_LESS, depth_write=1, y_
     d.blend = blend
     d.band_rows = band_rows
     d.flags = flags
+    d.primitives = primitives
     return d
 
 
@@ -386,6 +387,64 @@ def soup_frame(seed=0, width=1920, height=1080, ntris=200_000, area_lo=1.0, area
                      [TargetSpec("color", width, height, abi.FMT_RGBA8, 0),
                       TargetSpec("depth", width, height, abi.FMT_R32F, 1.0)], [p],
                      {"seed": seed, "kind": "soup"})
+
+
+def lines_frame(seed=0, width=640, height=360, nlines=5000, prims=abi.PRIM_LINE_LIST, len_lo=1.0, len_hi=400.0,
+                extent=1.2, perspective=False, alpha=False, **desc):
+    """Clip-space line soup (LineList), or the same vertices drawn as
+    LineTriangleList: end points around centres ~U[-extent, extent]^2,
+    screen lengths log-uniform in [len_lo, len_hi] px, z in [0.05, 0.95],
+    per-vertex RGBA8 colours, a seeded-permutation u32 index buffer, RGBA8 +
+    f32 depth, LESS_WRITE.  `perspective` gives each vertex a w in [0.5, 2]
+    (and z beyond the clip range for some); `alpha` blends src-over."""
+    rng = np.random.default_rng(seed)
+    per = 2 if prims == abi.PRIM_LINE_LIST else 3
+    nv = nlines * per
+    cen = np.repeat(rng.uniform(-extent, extent, (nlines, 2)), per, axis=0)
+    ln = np.exp(rng.uniform(math.log(len_lo), math.log(len_hi), nv))
+    th = rng.uniform(0, 2 * math.pi, nv)
+    x = cen[:, 0] + 0.5 * ln * np.cos(th) * (2.0 / width)
+    y = cen[:, 1] + 0.5 * ln * np.sin(th) * (2.0 / height)
+    z = rng.uniform(0.05, 0.95, nv)
+    w = np.ones(nv)
+    if perspective:
+        w = rng.uniform(0.5, 2.0, nv)
+        z = rng.uniform(-0.3, 1.3, nv)
+    clip = np.stack([x * w, y * w, z * w, w], axis=-1).astype(np.float32)
+    col = rng.integers(0, 256, (nv, 4), dtype=np.uint8)
+    col[:, 3] = rng.integers(32, 256, nv, dtype=np.uint8) if alpha else 255
+    perm = rng.permutation(nv).astype(np.uint32)
+    vb = np.empty((nv, 20), dtype=np.uint8)
+    vb[perm] = np.concatenate([clip.view(np.uint8).reshape(nv, 16), col], axis=1)
+    u = abi.VColorUniforms()
+    u.mvp = f32mat(np.eye(4))
+    kw = dict(cull=abi.CULL_NONE, primitives=prims, blend=abi.BLEND_ALPHA if alpha else abi.BLEND_REPLACE)
+    kw.update(desc)
+    p = PassSpec(make_desc(abi.SHADER_VCOLOR, **kw), layout(20, position=0, color=16), vb.reshape(-1), nv, perm, u,
+                 pixel="color", depth="depth")
+    return FrameSpec("lines%dx%d_%d_p%d" % (width, height, nlines, prims),
+                     [TargetSpec("color", width, height, abi.FMT_RGBA8, 0),
+                      TargetSpec("depth", width, height, abi.FMT_R32F, 1.0)], [p],
+                     {"seed": seed, "kind": "lines"})
+
+
+def wireframe_frame(seed=0, width=640, height=480, lon=48, lat=24, fmt=abi.FMT_BGRA8, aa_level=0):
+    """The wireframes example's pipeline (examples/wireframes.rs): a mesh drawn
+    as LineTriangleList, flat red, BGRA8 colour target, no depth target (Empty,
+    so no depth test and no depth write); here a UV sphere with a seeded
+    rotation."""
+    rng = np.random.default_rng(seed)
+    pos, nrm, _, idx = uv_sphere(lon, lat)
+    buf, stride, offs = pack_vertices(pos, nrm)
+    mvp = perspective_lh_zo(1.3, width / height, 0.01, 100.0) @ translation(0, 0, 3.0) @ quat_rotation(rng)
+    u = abi.FlatUniforms()
+    u.mvp = f32mat(mvp)
+    u.color = (C.c_float * 4)(1.0, 0.0, 0.0, 1.0)
+    p = PassSpec(make_desc(abi.SHADER_FLAT, depth_test=abi.TEST_NONE, depth_write=0, cull=abi.CULL_NONE,
+                           aa_level=aa_level, primitives=abi.PRIM_LINE_TRIANGLE_LIST),
+                 layout(stride, position=offs[0], normal=offs[1]), buf, len(pos), idx, u, pixel="color", depth=None)
+    return FrameSpec("wireframe%dx%d_%d" % (width, height, len(idx) // 3),
+                     [TargetSpec("color", width, height, fmt, 0)], [p], {"seed": seed, "kind": "wireframe"})
 
 
 def clip_triangles_frame(clip, colors, width, height, indices=None, pixel_fmt=abi.FMT_RGBA8, depth_clear=1.0,

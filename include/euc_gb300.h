@@ -70,6 +70,17 @@ enum euc_format {
     EUC_FMT_R32F = 4   /* f32                                                  */
 };
 
+/* Source layouts for texture ingest: the image crate's 8-bit pixel types
+ * and f32.                                                                  */
+enum euc_src_format {
+    EUC_SRC_RGBA8 = 0,       /* r,g,b,a                                        */
+    EUC_SRC_BGRA8 = 1,       /* b,g,r,a                                        */
+    EUC_SRC_RGB8 = 2,        /* r,g,b                                          */
+    EUC_SRC_LUMA8 = 3,       /* l                                              */
+    EUC_SRC_LUMA_ALPHA8 = 4, /* l,a                                            */
+    EUC_SRC_R32F = 5         /* f32                                            */
+};
+
 /* Shader kinds: device functors that mirror the Pipeline impls of euc's
  * examples (vertex -> fragment -> blend).                                   */
 enum euc_shader {
@@ -110,6 +121,14 @@ enum euc_wrap {
  * synchronisation per render (to size the lists).                          */
 #define EUC_FLAG_ORDERED 2u
 
+/* `Pipeline::Primitives` (primitives.rs): how the vertex stream is grouped
+ * and which rasteriser draws it.                                           */
+enum euc_primitives {
+    EUC_PRIM_TRIANGLE_LIST = 0,      /* TriangleList: 0 1 2 | 3 4 5 (primitives.rs:18-44)   */
+    EUC_PRIM_LINE_TRIANGLE_LIST = 1, /* LineTriangleList: lines 0-1, 1-2, 2-0 (:46-77)      */
+    EUC_PRIM_LINE_LIST = 2           /* LineList: lines 0-1, 2-3 (:79-104)                  */
+};
+
 /* Mirrors the mode methods of `Pipeline` (pipeline.rs:178-209).            */
 typedef struct euc_pipeline_desc {
     uint32_t shader;      /* enum euc_shader                                  */
@@ -126,6 +145,7 @@ typedef struct euc_pipeline_desc {
     uint32_t blend;       /* enum euc_blend                                   */
     uint32_t band_rows;   /* EUC_BANDS_PAR, EUC_BANDS_SEQ or an explicit height */
     uint32_t flags;       /* EUC_FLAG_*                                       */
+    uint32_t primitives;  /* enum euc_primitives (Pipeline::Primitives)       */
 } euc_pipeline_desc;
 
 /* A 2-D target (Buffer2d, buffer.rs:183-219): row-major, y*pitch + x*bpp. */
@@ -264,6 +284,7 @@ typedef struct euc_tuning {
     uint32_t raster_warp_rows;     /* (primitive, row) items a warp claims at once, 32..256, x32 (256) */
     uint32_t chunk_group;          /* 256-pixel chunks per scene lookup in init/resolve (adaptive)   */
     uint32_t chunk_blocks_per_sm;  /* init/resolve grid cap per SM (16)                              */
+    uint32_t raster_probe;         /* 1: read a key before its atomicMin, 2: atomics only (default)  */
 } euc_tuning;
 int euc_ctx_set_tuning(euc_ctx *ctx, const euc_tuning *tuning);
 int euc_ctx_get_tuning(euc_ctx *ctx, euc_tuning *tuning);
@@ -318,6 +339,30 @@ typedef struct euc_graph euc_graph;
 int euc_graph_create(euc_ctx *ctx, const euc_scene *scenes, size_t n, euc_graph **out);
 int euc_graph_launch(euc_graph *graph, void *stream);
 int euc_graph_destroy(euc_graph *graph);
+
+/* Texture ingest: `Buffer::from_texture` of an `image::ImageBuffer`
+ * (buffer.rs:32-58, texture.rs:321-344), done on the device.  Converts
+ * width x height texels of `src_format` (rows `src_pitch` bytes apart, in
+ * host or device memory) into `dst` (device memory, rows `dst_pitch` bytes
+ * apart) in a sampler layout: RGBA8 for the 8-bit sources, as image's
+ * to_rgba8 expands them (grey -> l,l,l,255; grey+alpha -> l,l,l,a;
+ * RGB -> alpha 255; BGRA reordered), and R32F for R32F.  A host source is
+ * staged through the context and the call waits for `stream`; a device
+ * source is converted in order on `stream`.  No counterpart in euc beyond
+ * the two calls it stands for.                                              */
+int euc_texture_ingest(euc_ctx *ctx, const void *src, uint32_t width, uint32_t height, uint64_t src_pitch,
+                       uint32_t src_format, void *dst, uint64_t dst_pitch, void *stream);
+
+/* Nearest sampling of an N-dimensional texture (N = 1..4): what
+ * `Nearest::sample` (sampler/nearest.rs:27-33) returns after the wrap of
+ * sampler/mod.rs:100-179 (`wrap`: euc_wrap), `Denormalize` per axis
+ * (math.rs:40-60) and the linear index of `Buffer<T, N>` (buffer.rs:85-100,
+ * axis 0 fastest).  `texels`: packed texels of `texel_bytes` (1..16) each,
+ * `size[ndim]` of them per axis; `queries`: `count` points of `ndim` f32;
+ * the texel of each point is copied to `out` (count * texel_bytes bytes).
+ * All three are device memory; ordered on `stream` of the current device.  */
+int euc_sample_nearest(const void *texels, uint32_t ndim, const uint32_t *size, uint32_t texel_bytes, uint32_t wrap,
+                       const float *queries, uint64_t count, void *out, void *stream);
 
 /* euc_render without a context and without any allocation.  No counterpart in
  * euc: it exists for callers that may not allocate device memory, such as an

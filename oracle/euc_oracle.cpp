@@ -1,4 +1,5 @@
-// euc_oracle.cpp — CPU restatement of euc 0.6.0's triangle pipeline.
+// euc_oracle.cpp — CPU restatement of euc 0.6.0's triangle pipeline (and its
+// line rasteriser).
 //
 // TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU pipeline:
 // only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs may
@@ -63,6 +64,60 @@ inline float rem_euclid(float x, float m) {
 
 inline uint64_t clamp_u64(uint64_t v, uint64_t lo, uint64_t hi) {
     return v < lo ? lo : (v > hi ? hi : v);
+}
+
+// `f as isize` (saturating, NaN -> 0), isize = i64.
+inline int64_t as_isize(float v) {
+    if (std::isnan(v)) return 0;
+    if (v >= 9.2233720368547758e18f) return INT64_MAX;
+    if (v <= -9.2233720368547758e18f) return INT64_MIN;
+    return (int64_t)v;
+}
+// f32::clamp with ordered, non-NaN bounds: a NaN input stays NaN.
+inline float fclamp(float v, float lo, float hi) { return v < lo ? lo : (v > hi ? hi : v); }
+// isize subtraction and abs wrap (overflow checks are off in euc's profiles).
+inline int64_t wsub(int64_t a, int64_t b) { return (int64_t)((uint64_t)a - (uint64_t)b); }
+inline int64_t wabs(int64_t a) { return a < 0 ? (int64_t)(0 - (uint64_t)a) : a; }
+
+// clipline 0.2 (a dependency of euc, not in the reference tree; its exact
+// pixel sequence is not pinned here).  Restated as: the pixels of the
+// Bresenham line from (x1, y1) to (x2, y2), both ends included, that lie in
+// the inclusive window [wx1, wx2] x [wy1, wy2] (clipline's window clipping
+// keeps exactly the unclipped line's pixels inside it).  The major axis is x
+// when |dx| >= |dy|; after i major steps the minor offset is
+//     m(i) = floor((2 |dminor| i + |dmajor| - 1) / (2 |dmajor|)),
+// which is the classic error-term loop (error 2|dminor| - |dmajor|, minor
+// step while the error is > 0).  Lines with |dx| or |dy| >= 2^30 draw
+// nothing.
+template <class Plot>
+void bresenham_clipped(int64_t x1, int64_t y1, int64_t x2, int64_t y2, int64_t wx1, int64_t wy1, int64_t wx2,
+                       int64_t wy2, Plot plot) {
+    if (wx2 < wx1 || wy2 < wy1) return;
+    const int64_t lim = (int64_t)1 << 30;
+    if (x1 <= -lim || x1 >= lim || x2 <= -lim || x2 >= lim || y1 <= -lim || y1 >= lim || y2 <= -lim || y2 >= lim)
+        return;
+    const int64_t dx = x2 - x1, dy = y2 - y1;
+    const bool xmaj = (dx < 0 ? -dx : dx) >= (dy < 0 ? -dy : dy);
+    const int64_t a1 = xmaj ? x1 : y1, a2 = xmaj ? x2 : y2, b1 = xmaj ? y1 : x1;
+    const int64_t dmaj = a2 - a1, dmin = xmaj ? dy : dx;
+    const int64_t amaj = dmaj < 0 ? -dmaj : dmaj, amin = dmin < 0 ? -dmin : dmin;
+    const int64_t smaj = dmaj < 0 ? -1 : 1, smin = dmin < 0 ? -1 : 1;
+    const int64_t wa1 = xmaj ? wx1 : wy1, wa2 = xmaj ? wx2 : wy2, wb1 = xmaj ? wy1 : wx1, wb2 = xmaj ? wy2 : wx2;
+    // major steps whose major coordinate lies in the window
+    int64_t i_lo, i_hi;
+    if (smaj > 0) { i_lo = wa1 - a1; i_hi = wa2 - a1; }
+    else { i_lo = a1 - wa2; i_hi = a1 - wa1; }
+    if (i_lo < 0) i_lo = 0;
+    if (i_hi > amaj) i_hi = amaj;
+    for (int64_t i = i_lo; i <= i_hi; ++i) {
+        // |dmajor|, |dminor| < 2^31: the numerator stays below 2^64
+        const int64_t m = amaj ? (int64_t)((2 * (uint64_t)amin * (uint64_t)i + (uint64_t)amaj - 1) /
+                                           (2 * (uint64_t)amaj))
+                               : 0;
+        const int64_t a = a1 + smaj * i, b = b1 + smin * m;
+        if (b < wb1 || b > wb2) continue;
+        plot(xmaj ? a : b, xmaj ? b : a);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -452,7 +507,8 @@ struct Band {
         }
     };
 
-    void msaa_fragment(uint64_t cx, uint64_t cy, const VData &gv, float *out) {  // pipeline.rs:477-494
+    template <class G>
+    void msaa_fragment(uint64_t cx, uint64_t cy, const G &gv, float *out) {  // pipeline.rs:477-494
         uint64_t slot = (cx + 1) + msaa_w * (cy + 1);
         float *f = &msaa_frag[slot * S::NF];
         if (msaa_key[slot] != primitive_count) {
@@ -464,7 +520,8 @@ struct Band {
         for (int i = 0; i < S::NF; ++i) out[i] = f[i];
     }
 
-    void emit_fragment(uint64_t x, uint64_t y, const VData &gv, float z) {  // pipeline.rs:529-578
+    template <class G>
+    void emit_fragment(uint64_t x, uint64_t y, const G &gv, float z) {  // pipeline.rs:529-578
         if (d.depth_write) depth.write_depth(x, y, z);
         if (d.pixel_write) {
             float frag[S::NF];
@@ -617,6 +674,57 @@ struct Band {
             }
         }
     }
+
+    // weighted_sum2 of a line's two vertex outputs (lines.rs:98-110)
+    struct LineVData {
+        bool use_x;
+        float sx0, sy0, norm;
+        const float *vo[2];
+        void operator()(float xf, float yf, float *out) const {
+            const float frac = (use_x ? xf - sx0 : yf - sy0) * norm;
+            for (int i = 0; i < S::NV; ++i) out[i] = vo[0][i] * (1.0f - frac) + vo[1][i] * frac;
+        }
+    };
+
+    // One line: Lines::rasterize (lines.rs:30-119) on this band.
+    void line(const float *hom_in[2], const float *out_in[2]) {
+        ++primitive_count;  // begin_primitive
+        ++triangles;        // primitives assembled
+        const float flip1 = d.y_axis == EUC_Y_UP ? -1.0f : 1.0f;
+        float euc[2][3], scr[2][2];
+        const float size_x = (float)tgt_size[0], size_y = (float)tgt_size[1];
+        for (int i = 0; i < 2; ++i) {
+            const float a0 = hom_in[i][0] * 1.0f, a1 = hom_in[i][1] * flip1, a2 = hom_in[i][2];
+            const float w = rmax(hom_in[i][3], 0.0001f);
+            euc[i][0] = a0 / w;
+            euc[i][1] = a1 / w;
+            euc[i][2] = a2 / w;
+            scr[i][0] = size_x * (euc[i][0] * 0.5f + 0.5f);
+            scr[i][1] = size_y * (euc[i][1] * -0.5f + 0.5f);
+        }
+        const float smin[2] = {(float)tgt_min[0], (float)tgt_min[1]};
+        const float smax[2] = {(float)tgt_max[0], (float)tgt_max[1]};
+        const int64_t x1 = as_isize(scr[0][0]), y1 = as_isize(scr[0][1]);
+        const int64_t x2 = as_isize(scr[1][0]), y2 = as_isize(scr[1][1]);
+        const int64_t wx1 = as_isize(fclamp(rmin(scr[0][0], scr[1][0]) + 0.0f, smin[0], smax[0]));
+        const int64_t wy1 = as_isize(fclamp(rmin(scr[0][1], scr[1][1]) + 0.0f, smin[1], smax[1]));
+        const int64_t wx2 = as_isize(fclamp(rmax(scr[0][0], scr[1][0]) + 1.0f, smin[0], smax[0]));
+        const int64_t wy2 = as_isize(fclamp(rmax(scr[0][1], scr[1][1]) + 1.0f, smin[1], smax[1]));
+        const bool use_x = wabs(wsub(x1, x2)) > wabs(wsub(y1, y2));
+        const float norm = 1.0f / (use_x ? scr[1][0] - scr[0][0] : scr[1][1] - scr[0][1]);
+        const LineVData gv{use_x, scr[0][0], scr[0][1], norm, {out_in[0], out_in[1]}};
+        bresenham_clipped(x1, y1, x2, y2, wx1, wy1, wx2 - 1, wy2 - 1, [&](int64_t xi, int64_t yi) {
+            const uint64_t x = (uint64_t)xi, y = (uint64_t)yi;
+            const float frac = (use_x ? (float)x - scr[0][0] : (float)y - scr[0][1]) * norm;
+            const float z = euc[0][2] + frac * (euc[1][2] - euc[0][2]);
+            if (!passes_z_clip(z)) return;
+            ++candidates;
+            if (test_fragment(x, y, z)) {
+                ++passed;
+                emit_fragment(x, y, gv, z);
+            }
+        });
+    }
 };
 
 inline uint64_t read_index(const uint32_t *idx, uint64_t i) { return idx ? idx[i] : i; }
@@ -638,10 +746,14 @@ int render_impl(const S &sh, const euc_pipeline_desc &d, const void *verts, uint
     const uint64_t n = idx ? nidx : nverts;
     for (uint64_t i = 0; i < n; ++i)
         if (read_index(idx, i) >= nverts) return EUC_ERR_INDEX_OOB;  // index.rs:53 panics before drawing
-    const uint64_t ntri = n / 3;  // TriangleList drops a trailing partial primitive
-    std::vector<float> clip(ntri * 3 * 4), vout(ntri * 3 * (uint64_t)S::NV);
+    // complete primitives of the stream; a trailing partial one is dropped
+    // (collect_primitive returns None, pipeline.rs:283)
+    const uint32_t per = d.primitives == EUC_PRIM_LINE_LIST ? 2 : 3;
+    const uint64_t ngroup = n / per;
+    const uint64_t nshade = ngroup * per;
+    std::vector<float> clip(nshade * 4), vout(nshade * (uint64_t)S::NV);
     const uint8_t *vb = (const uint8_t *)verts;
-    for (uint64_t i = 0; i < ntri * 3; ++i)
+    for (uint64_t i = 0; i < nshade; ++i)
         sh.vertex(vb + read_index(idx, i) * lay.stride, &clip[i * 4], &vout[i * S::NV]);
 
     const uint32_t level = d.aa_level > 6 ? 6 : d.aa_level;  // pipeline.rs:291-294
@@ -666,11 +778,31 @@ int render_impl(const S &sh, const euc_pipeline_desc &d, const void *verts, uint
             if (b >= nbands) break;
             uint64_t r0 = b * gr, r1 = r0 + gr < size[1] ? r0 + gr : size[1];
             Band<S> band(sh, d, pixel, depth, size, r0, r1, level);
-            for (uint64_t t = 0; t < ntri; ++t) {
-                const float *h[3] = {&clip[(t * 3 + 0) * 4], &clip[(t * 3 + 1) * 4], &clip[(t * 3 + 2) * 4]};
-                const float *o[3] = {&vout[(t * 3 + 0) * S::NV], &vout[(t * 3 + 1) * S::NV],
-                                     &vout[(t * 3 + 2) * S::NV]};
-                band.primitive(h, o);
+            if (d.primitives == EUC_PRIM_TRIANGLE_LIST) {
+                for (uint64_t t = 0; t < ngroup; ++t) {
+                    const float *h[3] = {&clip[(t * 3 + 0) * 4], &clip[(t * 3 + 1) * 4], &clip[(t * 3 + 2) * 4]};
+                    const float *o[3] = {&vout[(t * 3 + 0) * S::NV], &vout[(t * 3 + 1) * S::NV],
+                                         &vout[(t * 3 + 2) * S::NV]};
+                    band.primitive(h, o);
+                }
+            } else {
+                // LineList: (0 1) (2 3) ...; LineTriangleList: (a b) (b c) (c a)
+                // per triangle (primitives.rs:46-104)
+                const uint64_t nlines = d.primitives == EUC_PRIM_LINE_LIST ? ngroup : 3 * ngroup;
+                for (uint64_t l = 0; l < nlines; ++l) {
+                    uint64_t e0, e1;
+                    if (d.primitives == EUC_PRIM_LINE_LIST) {
+                        e0 = 2 * l;
+                        e1 = 2 * l + 1;
+                    } else {
+                        const uint64_t t = l / 3, k = l % 3;
+                        e0 = 3 * t + k;
+                        e1 = 3 * t + (k + 1) % 3;
+                    }
+                    const float *h[2] = {&clip[e0 * 4], &clip[e1 * 4]};
+                    const float *o[2] = {&vout[e0 * S::NV], &vout[e1 * S::NV]};
+                    band.line(h, o);
+                }
             }
             cnt.candidates += band.candidates;
             cnt.passed += band.passed;
@@ -703,6 +835,7 @@ int oracle_render(const euc_pipeline_desc *d, const void *uniforms, size_t usize
                   const void *verts, size_t nverts, const uint32_t *idx, size_t nidx, const euc_target *pixel,
                   const euc_target *depth, int threads, oracle_stats *st) {
     if (!d || !lay || !uniforms) return EUC_ERR_INVALID;
+    if (d->primitives > EUC_PRIM_LINE_LIST) return EUC_ERR_INVALID;
     if (nverts && !verts) return EUC_ERR_INVALID;
     Target px(pixel), dp(depth);
     if (d->pixel_write && px.data && fmt_bpp(px.fmt) == 0) return EUC_ERR_INVALID;
@@ -734,6 +867,51 @@ int oracle_render(const euc_pipeline_desc *d, const void *uniforms, size_t usize
         st->passed = cnt.passed;
     }
     return rc;
+}
+
+// N-D nearest sampling (sampler/nearest.rs:27-33, math.rs:40-60,
+// buffer.rs:85-100) after the wrap of sampler/mod.rs:100-179.
+int oracle_sample_nearest(const void *texels, uint32_t ndim, const uint32_t *size, uint32_t tb, uint32_t wrap,
+                          const float *queries, uint64_t count, void *out) {
+    if (!size || ndim < 1 || ndim > 4 || tb < 1 || tb > 16 || wrap > EUC_WRAP_MIRROR) return EUC_ERR_INVALID;
+    for (uint32_t a = 0; a < ndim; ++a)
+        if (size[a] < 1) return EUC_ERR_INVALID;
+    for (uint64_t i = 0; i < count; ++i) {
+        uint64_t lin = 0, factor = 1;
+        for (uint32_t a = 0; a < ndim; ++a) {
+            const float e = wrap_coord(wrap, queries[i * ndim + a]);
+            uint64_t idx = as_usize(rmax(e * (float)size[a], 0.0f));  // Denormalize::denormalize_to
+            if (idx > size[a] - 1u) idx = size[a] - 1u;
+            lin += idx * factor;  // Buffer::linear_index
+            factor *= size[a];
+        }
+        std::memcpy((uint8_t *)out + i * tb, (const uint8_t *)texels + lin * tb, tb);
+    }
+    return EUC_OK;
+}
+
+// Texture ingest: image's to_rgba8 expansion of the 8-bit layouts into RGBA8
+// texels, f32 copied as is (texture.rs:321-344 read through Buffer::from_texture).
+int oracle_texture_ingest(const void *src, uint32_t w, uint32_t h, uint64_t spitch, uint32_t fmt, void *dst,
+                          uint64_t dpitch) {
+    static const uint32_t bpp[6] = {4, 4, 3, 1, 2, 4};
+    if (fmt > EUC_SRC_R32F) return EUC_ERR_INVALID;
+    for (uint32_t y = 0; y < h; ++y)
+        for (uint32_t x = 0; x < w; ++x) {
+            const uint8_t *p = (const uint8_t *)src + y * spitch + (uint64_t)x * bpp[fmt];
+            uint8_t *q = (uint8_t *)dst + y * dpitch + 4ull * x;
+            uint8_t px[4];
+            switch (fmt) {
+            case EUC_SRC_RGBA8: px[0] = p[0]; px[1] = p[1]; px[2] = p[2]; px[3] = p[3]; break;
+            case EUC_SRC_BGRA8: px[0] = p[2]; px[1] = p[1]; px[2] = p[0]; px[3] = p[3]; break;
+            case EUC_SRC_RGB8: px[0] = p[0]; px[1] = p[1]; px[2] = p[2]; px[3] = 255; break;
+            case EUC_SRC_LUMA8: px[0] = px[1] = px[2] = p[0]; px[3] = 255; break;
+            case EUC_SRC_LUMA_ALPHA8: px[0] = px[1] = px[2] = p[0]; px[3] = p[1]; break;
+            default: std::memcpy(px, p, 4); break;
+            }
+            std::memcpy(q, px, 4);
+        }
+    return EUC_OK;
 }
 
 // Scalar helpers exposed for known-answer tests of Rust semantics.

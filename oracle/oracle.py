@@ -45,6 +45,12 @@ def lib():
         L.oracle_sample.restype = None
         L.oracle_sample.argtypes = [C.POINTER(abi.Sampler), C.c_float, C.c_float, C.POINTER(C.c_float)]
         L.oracle_hw_threads.restype = C.c_int
+        L.oracle_sample_nearest.restype = C.c_int
+        L.oracle_sample_nearest.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32), C.c_uint32, C.c_uint32,
+                                            C.c_void_p, C.c_uint64, C.c_void_p]
+        L.oracle_texture_ingest.restype = C.c_int
+        L.oracle_texture_ingest.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, C.c_void_p,
+                                            C.c_uint64]
         _lib = L
     return _lib
 
@@ -98,6 +104,34 @@ def sample(sampler, u, v):
     out = (C.c_float * 4)()
     lib().oracle_sample(C.byref(sampler), u, v, out)
     return np.array(list(out), dtype=np.float32)
+
+
+def sample_nearest(texels, queries, wrap):
+    """N-D nearest sampling: texels (s_{N-1}, ..., s_0, texel bytes...) numpy
+    array, axis 0 fastest; queries (count, N) f32.  Returns (count, texel
+    bytes) uint8, or raises on a refused shape."""
+    ndim = queries.shape[1]
+    tex = np.ascontiguousarray(texels)
+    size = (C.c_uint32 * ndim)(*[tex.shape[ndim - 1 - a] for a in range(ndim)])
+    tb = tex.itemsize * int(np.prod(tex.shape[ndim:], dtype=np.int64))
+    q = np.ascontiguousarray(queries, dtype=np.float32)
+    out = np.zeros((len(q), tb), dtype=np.uint8)
+    rc = lib().oracle_sample_nearest(tex.ctypes.data, ndim, size, tb, wrap, q.ctypes.data, len(q), out.ctypes.data)
+    if rc:
+        raise ValueError("oracle_sample_nearest: %d" % rc)
+    return out
+
+
+def texture_ingest(src, fmt):
+    """Image rows (h, w, channels) uint8 or (h, w) float32 -> (h, w, 4) uint8
+    RGBA8 texels (or the f32 bits as 4 bytes)."""
+    a = np.ascontiguousarray(src)
+    h, w = a.shape[:2]
+    out = np.zeros((h, w, 4), dtype=np.uint8)
+    rc = lib().oracle_texture_ingest(a.ctypes.data, w, h, a.strides[0], fmt, out.ctypes.data, out.strides[0])
+    if rc:
+        raise ValueError("oracle_texture_ingest: %d" % rc)
+    return out
 
 
 def run_frame(frame, threads=1):

@@ -48,7 +48,11 @@ def load(path):
     targets = [scenes.TargetSpec(n, w, h, f, c) for n, w, h, f, c in meta["targets"]]
     passes = []
     for k, pm in enumerate(meta["passes"]):
-        desc = abi.PipelineDesc.from_buffer_copy(z["p%d_desc" % k].tobytes())
+        raw = z["p%d_desc" % k].tobytes()
+        # fixtures written before the desc grew its `primitives` field hold a
+        # shorter struct: the missing fields are 0 (TriangleList)
+        raw += bytes(max(0, C.sizeof(abi.PipelineDesc) - len(raw)))
+        desc = abi.PipelineDesc.from_buffer_copy(raw)
         lay = abi.VertexLayout.from_buffer_copy(z["p%d_layout" % k].tobytes())
         uni = abi.UNIFORMS_FOR_SHADER[pm["shader"]].from_buffer_copy(z["p%d_uniforms" % k].tobytes())
         idx = z["p%d_indices" % k] if ("p%d_indices" % k) in z.files else None

@@ -120,6 +120,10 @@ def _unindexed():
     return make
 
 
+def _lines(seed=31, prims=abi.PRIM_LINE_LIST, **kw):
+    return lambda: scenes.lines_frame(seed=seed, prims=prims, **kw)
+
+
 CASES = {
     "sphere640x480": (_sphere(seed=3), 0),
     "sphere_small_odd": (_sphere(seed=5, width=97, height=61, lon=24, lat=12), 0),
@@ -162,6 +166,19 @@ CASES = {
     "alpha_soup_rgb8": (_fmt(_soup(seed=26, alpha=True), abi.FMT_RGB8), 0),
     "alpha_soup_bgra8": (_fmt(_soup(seed=27, alpha=True), abi.FMT_BGRA8), 0),
     # replace blends forced through the ordered path must give the same bytes
+    # lines (lines.rs) and the wireframe example's LineTriangleList pipeline
+    "lines_less": (_lines(), 0),
+    "lines_tri_list": (_lines(seed=32, prims=abi.PRIM_LINE_TRIANGLE_LIST, nlines=2000), 0),
+    "lines_perspective_zclip": (_lines(seed=33, perspective=True), 0),
+    "lines_perspective_noclip": (_lines(seed=34, perspective=True, z_clip=None, depth_test=abi.TEST_NONE), 0),
+    "lines_equal_pass": (_clear(_lines(seed=35, depth_test=abi.TEST_EQUAL, depth_write=0), "depth", 0.5), 0),
+    "lines_msaa1_bands": (_lines(seed=36, width=333, height=177, aa_level=1, band_rows=9), 0),
+    "lines_msaa2": (_lines(seed=37, aa_level=2), 0),
+    "lines_long_offscreen": (_lines(seed=38, nlines=300, len_lo=500.0, len_hi=5000.0, extent=2.0), 0),
+    "lines_alpha": (_lines(seed=39, alpha=True), 0),
+    "lines_ordered": (_lines(seed=40, flags=abi.FLAG_ORDERED), 0),
+    "wireframe_bgra8": (lambda: scenes.wireframe_frame(seed=41), 0),
+    "wireframe_msaa1_rgba8": (lambda: scenes.wireframe_frame(seed=42, fmt=abi.FMT_RGBA8, aa_level=1), 0),
     "ordered_sphere": (_mod(_sphere(seed=3), flags=abi.FLAG_ORDERED), 0),
     "ordered_soup_less": (_soup(seed=1, flags=abi.FLAG_ORDERED), 0),
     "ordered_soup_equal": (_clear(_soup(seed=3, depth_test=abi.TEST_EQUAL, flags=abi.FLAG_ORDERED), "depth", 0.5), 0),

@@ -121,6 +121,8 @@ SHAPES = [
     dict(chunk_group=1, chunk_blocks_per_sm=1),
     dict(chunk_group=7, chunk_blocks_per_sm=3),
     dict(chunk_group=1024, chunk_blocks_per_sm=64, raster_warp_rows=224, raster_blocks_per_sm=2),
+    dict(raster_probe=2),
+    dict(raster_probe=1, raster_warp_rows=64),
 ]
 
 
@@ -150,7 +152,7 @@ def test_launch_shapes_do_not_change_results(which):
 
 @pytest.mark.parametrize("bad", [dict(raster_warp_rows=48), dict(raster_warp_rows=288),
                                  dict(raster_blocks_per_sm=65), dict(chunk_group=1025),
-                                 dict(chunk_blocks_per_sm=100)])
+                                 dict(chunk_blocks_per_sm=100), dict(raster_probe=3)])
 def test_invalid_launch_shapes_are_refused(bad):
     ctx = capi.Context(0)
     try:

@@ -4,7 +4,7 @@ import pytest
 
 from euc_gb300 import abi, scenes
 from euc_gb300.pipeline import (AaMode, Buffer2d, CoordinateMode, CullMode, DepthMode, Empty, IndexedVertices,
-                                Pipeline, PixelMode)
+                                LineList, LineTriangleList, Pipeline, PixelMode, TriangleList)
 
 
 class Sphere(Pipeline):
@@ -65,6 +65,31 @@ def test_desc_from_mode_methods():
     assert AaMode.Msaa(2).level == 2
 
 
+class Wireframe(Pipeline):
+    """examples/wireframes.rs: LineTriangleList, flat red, BGRA8, no depth."""
+    SHADER = abi.SHADER_FLAT
+    Primitives = LineTriangleList
+
+    def __init__(self, spec):
+        self.spec = spec
+
+    def rasterizer_config(self):
+        return CullMode.None_
+
+    def uniforms(self):
+        return self.spec.uniforms
+
+    def vertex_layout(self):
+        return self.spec.layout
+
+
+def test_primitive_kinds_set_the_desc():
+    spec = scenes.wireframe_frame(seed=1).passes[0]
+    assert Wireframe(spec).desc().primitives == abi.PRIM_LINE_TRIANGLE_LIST
+    assert Sphere(scenes.sphere_frame(seed=1).passes[0]).desc().primitives == abi.PRIM_TRIANGLE_LIST
+    assert (TriangleList.KIND, LineTriangleList.KIND, LineList.KIND) == (0, 1, 2)
+
+
 def test_buffer2d_fill_and_clear():
     b = Buffer2d.fill([5, 3], 0x11223344, fmt=abi.FMT_RGBA8)
     assert b.size() == [5, 3] and (b.data[..., 0] == 0x44).all()
@@ -111,3 +136,15 @@ def test_render_errors_like_euc_panics():
         Sphere(spec).render(IndexedVertices(spec.indices, spec.vertices), Buffer2d.fill([32, 32], 0, fmt=abi.FMT_RGB8),
                             Buffer2d.fill([32, 31], 1.0))
     assert e.value.code == abi.ERR_SIZE_MISMATCH
+
+
+@pytest.mark.gpu
+def test_wireframe_render_matches_oracle():
+    from oracle import oracle
+    frame = scenes.wireframe_frame(seed=9, width=320, height=240)
+    ref, _, _ = oracle.run_frame(frame)
+    spec = frame.passes[0]
+    color = Buffer2d.fill([320, 240], 0, fmt=abi.FMT_BGRA8)
+    Wireframe(spec).render(IndexedVertices(spec.indices, spec.vertices), color, Empty())
+    assert np.array_equal(color.data, ref["color"])
+    assert (color.data[..., 2] == 255).sum() > 1000  # red lines in BGRA
