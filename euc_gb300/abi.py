@@ -33,6 +33,7 @@ STATUS_NAMES = {
 TEST_NONE, TEST_LESS, TEST_EQUAL, TEST_GREATER = 0, 1, 2, 3
 PRIM_TRIANGLE_LIST, PRIM_LINE_TRIANGLE_LIST, PRIM_LINE_LIST = 0, 1, 2
 SRC_RGBA8, SRC_BGRA8, SRC_RGB8, SRC_LUMA8, SRC_LUMA_ALPHA8, SRC_R32F = 0, 1, 2, 3, 4, 5
+GEOM_NONE, GEOM_SUBDIVIDE, GEOM_SHRINK, GEOM_DUPLICATE, GEOM_DISCARD = 0, 1, 2, 3, 4
 CULL_NONE, CULL_BACK, CULL_FRONT = 0, 1, 2
 Y_DOWN, Y_UP = 0, 1
 LEFT, RIGHT = 0, 1
@@ -59,6 +60,7 @@ class PipelineDesc(C.Structure):
         ("z_clip", C.c_uint32), ("z_clip_min", C.c_float), ("z_clip_max", C.c_float),
         ("aa_level", C.c_uint32), ("cull", C.c_uint32), ("blend", C.c_uint32),
         ("band_rows", C.c_uint32), ("flags", C.c_uint32), ("primitives", C.c_uint32),
+        ("geometry", C.c_uint32), ("geometry_param", C.c_float),
     ]
 
 

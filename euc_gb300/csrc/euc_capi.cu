@@ -44,6 +44,7 @@ struct euc_ctx {
     DevBuf clip, vdata, recs, rows, chunk_sums, live_tri, live_rowoff, totals, vbuf, err, stats, cov;
     DevBuf obsum, frags;  // ordered path: pixel-scan block sums, fragment lists
     DevBuf plan;          // k_plan: k_init and k_resolve chunk bases (2 x (scenes + 1))
+    DevBuf galive;        // geometry stage: 1 per output slot that holds a triangle
     int raster_blocks = 0;  // resident k_raster blocks per SM
     euc_tuning tune{};      // launch-shape overrides (0 = default)
     // buffers used by euc_render_host
@@ -154,7 +155,9 @@ int plan_scene(const euc_scene &sc, Plan &p) {
     const euc_pipeline_desc &d = sc.desc;
     if (d.shader >= EUC_SHADER_COUNT) return EUC_ERR_INVALID;
     if (d.depth_test > EUC_TEST_GREATER || d.cull > EUC_CULL_FRONT || d.y_axis > EUC_Y_UP) return EUC_ERR_INVALID;
-    if (d.blend > EUC_BLEND_ALPHA || d.primitives > EUC_PRIM_LINE_LIST) return EUC_ERR_INVALID;
+    if (d.blend > EUC_BLEND_ALPHA || d.primitives > EUC_PRIM_LINE_LIST || d.geometry > EUC_GEOM_DISCARD)
+        return EUC_ERR_INVALID;
+    if (d.geometry != EUC_GEOM_NONE && d.primitives != EUC_PRIM_TRIANGLE_LIST) return EUC_ERR_INVALID;
     const size_t need = uniforms_size_for(d.shader);
     if (!sc.uniforms || sc.uniforms_size < need) return EUC_ERR_INVALID;
     const euc_vertex_layout &l = sc.layout;
@@ -245,6 +248,15 @@ int plan_scene(const euc_scene &sc, Plan &p) {
     } else {  // three lines per complete triangle
         s.ntris = (uint32_t)(3 * (nstream / 3));
         s.ngroups = (uint32_t)(3 * ((nstream + 2) / 3));
+    }
+    s.geom = d.geometry;
+    s.gparam = d.geometry_param;
+    if (s.geom != EUC_GEOM_NONE) {  // setup sees the geometry stage's output slots
+        s.gratio = geometry_ratio(s.geom);
+        s.ntin = (uint32_t)(nstream / 3);
+        s.ngin = (uint32_t)((nstream + 2) / 3);
+        if ((uint64_t)s.gratio * s.ntin >= 0x3FFFFFFFull) return EUC_ERR_CAPACITY;
+        s.ntris = s.ngroups = s.gratio * s.ntin;
     }
     s.W = W;
     s.H = H;
@@ -369,6 +381,25 @@ void launch_vertex(const SceneDev *sc, const uint64_t *vb, int s0, int s1, uint6
 // rbase: the device chunk bases of k_plan; nblk: an upper bound of the
 // chunks of scenes [s0, s1) (their whole targets), which sizes the grid.
 template <class F>
+void launch_geometry(const SceneDev *sc, const uint64_t *gb, int s0, int s1, uint64_t blk0, uint64_t nblk, euc_ctx *ctx,
+                     cudaStream_t st) {
+    k_geometry<F><<<(unsigned)nblk, kBlock, 0, st>>>(sc, gb, s0, s1, blk0, (float4 *)ctx->clip.p, (float *)ctx->vdata.p,
+                                                     (uint8_t *)ctx->galive.p, (int *)ctx->err.p);
+}
+
+void dispatch_geometry(uint32_t shader, const SceneDev *sc, const uint64_t *gb, int s0, int s1, uint64_t blk0,
+                       uint64_t nblk, euc_ctx *ctx, cudaStream_t st) {
+    switch (shader) {
+    case EUC_SHADER_FLAT: launch_geometry<FlatFn>(sc, gb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_VCOLOR: launch_geometry<VColorFn>(sc, gb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_GOURAUD: launch_geometry<GouraudFn>(sc, gb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_TEXTURED: launch_geometry<TexturedFn>(sc, gb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_PHONG: launch_geometry<PhongFn>(sc, gb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_SHADOW: launch_geometry<ShadowFn>(sc, gb, s0, s1, blk0, nblk, ctx, st); break;
+    }
+}
+
+template <class F>
 void launch_resolve(const SceneDev *sc, const uint64_t *rbase, int s0, int s1, uint64_t nblk, euc_ctx *ctx,
                     cudaStream_t st) {
     if (!nblk) return;
@@ -471,6 +502,21 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
         pix += pad_up((uint64_t)p.d.W * p.d.H, kBlock);
         res += resolve_blocks(p.d);
     }
+    // geometry stage: its input threads, and its output vertices after every
+    // scene's vertex-stage outputs (the vertex launches cover only those)
+    const uint64_t vtx_stage = vtx;  // the vertex launches end here
+    std::vector<uint64_t> gin_base(ns);
+    uint64_t gin = 0;
+    for (int i = 0; i < ns; ++i) {
+        Plan &p = plans[i];
+        gin_base[i] = gin;
+        if (!p.d.geom) continue;
+        gin += pad_up(p.d.ngin, kBlock);
+        p.d.gvtx_base = vtx;
+        p.d.gvd_base = vd;
+        vtx += 3ull * p.d.ntris;
+        vd += 3ull * p.d.ntris * p.nv;
+    }
     if (tri >= 0x7FFFFFF0ull) return EUC_ERR_CAPACITY;  // visibility keys hold a 31-bit primitive id
     const uint64_t nchunks = tri / kBlock;
     const uint64_t nscan = (tri + kScanBlock - 1) / kScanBlock;
@@ -488,12 +534,14 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
     if ((rc = grow(ctx->stats, ns * sizeof(SceneStats)))) return rc;
     if ((rc = grow(ctx->cov, ns * sizeof(uint4)))) return rc;
     if ((rc = grow(ctx->plan, 2 * (ns + 1) * sizeof(uint64_t)))) return rc;
-    // staging: scene table | vtx bases | tri bases | resolve bases | uniforms
+    if (gin && (rc = grow(ctx->galive, tri))) return rc;
+    // staging: scene table | vtx bases | tri bases | resolve bases | geometry bases | uniforms
     const size_t off_sc = 0;
     const size_t off_vb = pad_up(ns * sizeof(SceneDev), 16);
     const size_t off_tb = off_vb + pad_up(ns * sizeof(uint64_t), 16);
     const size_t off_rb = off_tb + pad_up(ns * sizeof(uint64_t), 16);
-    size_t off_u = off_rb + pad_up(ns * sizeof(uint64_t), 16);
+    const size_t off_gb = off_rb + pad_up(ns * sizeof(uint64_t), 16);
+    size_t off_u = off_gb + pad_up(ns * sizeof(uint64_t), 16);
     std::vector<size_t> uoff(ns);
     for (int i = 0; i < ns; ++i) {
         uoff[i] = off_u;
@@ -512,7 +560,8 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
     uint8_t *h = (uint8_t *)(so ? so->host : slot->host);
     uint8_t *dv = (uint8_t *)(so ? so->dev : slot->dev);
     SceneDev *hsc = (SceneDev *)(h + off_sc);
-    uint64_t *hvb = (uint64_t *)(h + off_vb), *htb = (uint64_t *)(h + off_tb), *hrb = (uint64_t *)(h + off_rb);
+    uint64_t *hvb = (uint64_t *)(h + off_vb), *htb = (uint64_t *)(h + off_tb), *hrb = (uint64_t *)(h + off_rb),
+             *hgb = (uint64_t *)(h + off_gb);
     for (int i = 0; i < ns; ++i) {
         std::memcpy(h + uoff[i], plans[i].uniforms, plans[i].usize);
         plans[i].d.uniforms = dv + uoff[i];
@@ -520,11 +569,12 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
         hvb[i] = plans[i].d.vtx_base;
         htb[i] = plans[i].d.tri_base;
         hrb[i] = res_base[i];
+        hgb[i] = gin_base[i];
     }
     CUDA_TRY(cudaMemcpyAsync(dv, h, off_u, cudaMemcpyHostToDevice, st));
     const SceneDev *dsc = (const SceneDev *)(dv + off_sc);
     const uint64_t *dvb = (const uint64_t *)(dv + off_vb), *dtb = (const uint64_t *)(dv + off_tb),
-                   *drb = (const uint64_t *)(dv + off_rb);
+                   *drb = (const uint64_t *)(dv + off_rb), *dgb = (const uint64_t *)(dv + off_gb);
     CUDA_TRY(cudaMemsetAsync(ctx->err.p, 0, ns * sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(ctx->stats.p, 0, ns * sizeof(SceneStats), st));
     CUDA_TRY(cudaMemsetAsync(ctx->cov.p, 0xFF, ns * sizeof(uint4), st));  // empty rectangles
@@ -534,15 +584,27 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
         int b = a;
         while (b < ns && plans[b].d.shader == plans[a].d.shader) ++b;
         const uint64_t blk0 = plans[a].d.vtx_base / kBlock;
-        const uint64_t blk1 = (b < ns ? plans[b].d.vtx_base : vtx) / kBlock;
+        const uint64_t blk1 = (b < ns ? plans[b].d.vtx_base : vtx_stage) / kBlock;
         dispatch_vertex(plans[a].d.shader, dsc, dvb, a, b, blk0, blk1 - blk0, ctx, st);
         ctx->launches += blk1 > blk0;
+        a = b;
+    }
+    // geometry stage, one launch per shader kind that has one
+    for (int a = 0; a < ns && gin;) {
+        int b = a;
+        while (b < ns && plans[b].d.shader == plans[a].d.shader) ++b;
+        const uint64_t blk0 = gin_base[a] / kBlock, blk1 = (b < ns ? gin_base[b] : gin) / kBlock;
+        if (blk1 > blk0) {
+            dispatch_geometry(plans[a].d.shader, dsc, dgb, a, b, blk0, blk1 - blk0, ctx, st);
+            ctx->launches += 1;
+        }
         a = b;
     }
     cudaEvent_t e1 = prof_event(ctx, st);
     k_setup<<<(unsigned)nchunks, kBlock, 0, st>>>(dsc, dtb, ns, (const float4 *)ctx->clip.p, (TriRec *)ctx->recs.p,
                                                    (uint32_t *)ctx->rows.p, (uint2 *)ctx->chunk_sums.p, (int *)ctx->err.p,
-                                                   (SceneStats *)ctx->stats.p, (uint4 *)ctx->cov.p);
+                                                   (SceneStats *)ctx->stats.p, (uint4 *)ctx->cov.p,
+                                                   (const uint8_t *)ctx->galive.p);
     cudaEvent_t e2 = prof_event(ctx, st);
     k_scan<<<(unsigned)nscan, kBlock, 0, st>>>((const uint32_t *)ctx->rows.p, (const uint2 *)ctx->chunk_sums.p, tri,
                                                (uint32_t *)ctx->live_tri.p, (uint64_t *)ctx->live_rowoff.p,
@@ -821,18 +883,18 @@ struct euc_graph {
     cudaGraphExec_t exec = nullptr;
     int nscenes = 0;
     uint64_t launches = 0;   // kernels in the recorded batch
-    void *scratch[13] = {};  // the context's scratch pointers the graph was recorded with
+    void *scratch[14] = {};  // the context's scratch pointers the graph was recorded with
 };
 
 namespace {
 
 // The scratch buffers a recorded batch reads and writes.  A later render that
 // grows one of them moves it, and the graph may then no longer be launched.
-constexpr int kScratchBufs = 13;
+constexpr int kScratchBufs = 14;
 void scratch_ptrs(const euc_ctx *c, void *out[kScratchBufs]) {
     const DevBuf *b[kScratchBufs] = {&c->clip, &c->vdata,  &c->recs, &c->rows,  &c->chunk_sums,
                                      &c->live_tri, &c->live_rowoff, &c->totals, &c->vbuf, &c->err,
-                                     &c->stats, &c->cov, &c->plan};
+                                     &c->stats, &c->cov, &c->plan, &c->galive};
     for (int i = 0; i < kScratchBufs; ++i) out[i] = b[i]->p;
 }
 
@@ -1215,7 +1277,9 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
     }
     // order-dependent blends keep every fragment in lists whose size is only
     // known on the device; they need euc_render's growable buffers
-    if (p.d.keytype == KEY_ORDERED) return EUC_ERR_CAPACITY;
+    // ordered scenes size their fragment lists on the device; a geometry
+    // stage's output vertices need room beyond the fixed vertex array
+    if (p.d.keytype == KEY_ORDERED || p.d.geom != EUC_GEOM_NONE) return EUC_ERR_CAPACITY;
     if (p.d.nverts > kNaMaxVerts || p.d.ngroups > kNaMaxGroups || (uint64_t)p.d.W * p.d.H > kNaMaxPixels ||
         p.nv > (uint32_t)kNaMaxNV)
         return EUC_ERR_CAPACITY;
@@ -1245,7 +1309,8 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
     k_setup<<<(unsigned)(tri / kBlock), kBlock, 0, st>>>(dsc, zero_base, 1, (const float4 *)(a + kNaOffClip),
                                                           (TriRec *)(a + kNaOffRecs), (uint32_t *)(a + kNaOffRows),
                                                           (uint2 *)(a + kNaOffChunks), (int *)(a + kNaOffErr),
-                                                          (SceneStats *)(a + kNaOffStats), (uint4 *)(a + kNaOffCov));
+                                                          (SceneStats *)(a + kNaOffStats), (uint4 *)(a + kNaOffCov),
+                                                          nullptr);
     k_scan<<<(unsigned)((tri + kScanBlock - 1) / kScanBlock), kBlock, 0, st>>>(
         (const uint32_t *)(a + kNaOffRows), (const uint2 *)(a + kNaOffChunks), tri, (uint32_t *)(a + kNaOffLiveTri),
         (uint64_t *)(a + kNaOffLiveOff), (unsigned long long *)(a + kNaOffTotals));

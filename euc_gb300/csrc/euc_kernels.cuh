@@ -64,6 +64,14 @@ struct SceneDev {
     uint32_t pixel_write, depth_test, depth_write, yflip, zclip, cull, blend, keytype;
     float zmin, zmax;
     uint32_t shader, prim;    // enum euc_shader, enum euc_primitives
+    // geometry stage (geom != EUC_GEOM_NONE): k_geometry turns the ntin
+    // complete input triangles (ngin groups with the partial one) into
+    // gratio output slots each, written non-indexed at gvtx_base / gvd_base;
+    // setup and resolve then read those (slot lt: vertices 3 lt .. 3 lt + 2)
+    uint64_t gvtx_base, gvd_base;
+    uint32_t geom, gratio, ngin, ntin;
+    float gparam;
+    uint32_t pad1;
 };
 
 // Per-primitive record written by k_setup (128 bytes, 16-byte aligned).
@@ -176,6 +184,116 @@ __global__ void __launch_bounds__(kBlock) k_vertex(const SceneDev *__restrict__ 
     float *out = vdata + s.vd_base + v * F::NV;
 #pragma unroll
     for (int i = 0; i < F::NV; ++i) out[i] = vd[i];
+}
+
+// ---------------------------------------------------------------------------
+// k_geometry<F>: the built-in geometry stages (enum euc_geometry), one thread
+// per input triangle; outputs keep submission order (slot gratio * g + k).
+// ---------------------------------------------------------------------------
+__host__ __device__ inline uint32_t geometry_ratio(uint32_t g) {
+    return g == EUC_GEOM_SUBDIVIDE ? 4u : g == EUC_GEOM_DUPLICATE ? 2u : 1u;
+}
+
+// Output k of geometry `g` for the triangle (c, v); false when it emits
+// fewer than k + 1 triangles.
+template <int NV>
+EUC_DEV bool geometry_out(uint32_t g, float param, const float c[3][4], const float v[3][NV], int k, float oc[3][4],
+                          float ov[3][NV]) {
+    if (g == EUC_GEOM_SUBDIVIDE) {
+        // corners a, b, c and midpoints ab, bc, ca as (i, j) pairs: (i, i) is a corner
+        const int tri[4][3][2] = {{{0, 0}, {0, 1}, {2, 0}}, {{0, 1}, {1, 1}, {1, 2}},
+                                  {{2, 0}, {1, 2}, {2, 2}}, {{0, 1}, {1, 2}, {2, 0}}};
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const int p = tri[k][j][0], q = tri[k][j][1];
+            if (p == q) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) oc[j][i] = c[p][i];
+#pragma unroll
+                for (int i = 0; i < NV; ++i) ov[j][i] = v[p][i];
+            } else {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) oc[j][i] = c[p][i] * 0.5f + c[q][i] * 0.5f;
+#pragma unroll
+                for (int i = 0; i < NV; ++i) ov[j][i] = v[p][i] * 0.5f + v[q][i] * 0.5f;
+            }
+        }
+        return true;
+    }
+    if (g == EUC_GEOM_DISCARD) {
+        bool beyond = true;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) beyond = beyond && (c[j][2] / c[j][3] > param);
+        if (beyond) return false;
+    }
+    if (k > 0 && g != EUC_GEOM_DUPLICATE) return false;
+    float m[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) m[i] = ((c[0][i] + c[1][i]) + c[2][i]) / 3.0f;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) oc[j][i] = g == EUC_GEOM_SHRINK ? m[i] + (c[j][i] - m[i]) * param : c[j][i];
+        if (k == 1) oc[j][0] = c[j][0] + param * c[j][3];
+#pragma unroll
+        for (int i = 0; i < NV; ++i) ov[j][i] = v[j][i];
+    }
+    return true;
+}
+
+template <class F>
+__global__ void __launch_bounds__(kBlock) k_geometry(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ gin_base,
+                                                     int s_begin, int s_end, uint64_t blk_begin, float4 *__restrict__ clip,
+                                                     float *__restrict__ vdata, uint8_t *__restrict__ galive,
+                                                     int *__restrict__ err) {
+    __shared__ int s_scene;
+    const uint64_t pos = (blk_begin + blockIdx.x) * (uint64_t)kBlock;
+    if (threadIdx.x == 0) s_scene = s_begin + find_scene(gin_base + s_begin, s_end - s_begin, pos);
+    __syncthreads();
+    const int si = s_scene;
+    const SceneDev &s = sc[si];
+    const uint64_t g = pos + threadIdx.x - gin_base[si];
+    if (g >= s.ngin) return;
+    bool ok = true;
+    uint32_t vid[3] = {0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const uint64_t e = 3 * g + k;
+        if (e < s.nstream) {
+            const uint64_t id = s.idx ? (uint64_t)__ldg(s.idx + e) : e;
+            if (id >= s.nverts) ok = false;  // index.rs:53
+            vid[k] = (uint32_t)id;
+        }
+    }
+    if (!ok) atomicCAS(err + si, 0, EUC_ERR_INDEX_OOB);
+    if (g >= s.ntin) return;  // a trailing partial triangle has no output slots
+    const uint32_t R = s.gratio;
+    uint8_t *alive = galive + s.tri_base + (uint64_t)R * g;
+    float c[3][4], v[3][F::NV];
+    if (ok) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const float4 q = clip[s.vtx_base + vid[j]];
+            c[j][0] = q.x; c[j][1] = q.y; c[j][2] = q.z; c[j][3] = q.w;
+            const float *src = vdata + s.vd_base + (uint64_t)vid[j] * F::NV;
+#pragma unroll
+            for (int i = 0; i < F::NV; ++i) v[j][i] = src[i];
+        }
+    }
+    for (uint32_t k = 0; k < R; ++k) {
+        float oc[3][4], ov[3][F::NV];
+        const bool live = ok && geometry_out<F::NV>(s.geom, s.gparam, c, v, (int)k, oc, ov);
+        alive[k] = live ? 1 : 0;
+        if (!live) continue;
+        const uint64_t o = 3 * ((uint64_t)R * g + k);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            clip[s.gvtx_base + o + j] = make_float4(oc[j][0], oc[j][1], oc[j][2], oc[j][3]);
+            float *dst = vdata + s.gvd_base + (o + j) * F::NV;
+#pragma unroll
+            for (int i = 0; i < F::NV; ++i) dst[i] = ov[j][i];
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -327,7 +445,7 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
                                                   int nsc, const float4 *__restrict__ clip, TriRec *__restrict__ recs,
                                                   uint32_t *__restrict__ rows, uint2 *__restrict__ chunk_sums,
                                                   int *__restrict__ err, SceneStats *__restrict__ stats,
-                                                  uint4 *__restrict__ cov) {
+                                                  uint4 *__restrict__ cov, const uint8_t *__restrict__ galive) {
     __shared__ int s_scene;
     __shared__ uint32_t s_red[2][kBlock / 32];
     const uint64_t t = (uint64_t)blockIdx.x * kBlock + threadIdx.x;
@@ -344,22 +462,29 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
     } else if (lt < s.ngroups) {
         uint32_t vid[3] = {0, 0, 0};
         bool ok = true;
+        if (s.geom) {  // the geometry stage's output slot: checked and written by k_geometry
+            ok = galive[t] != 0;
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const uint64_t e = 3 * lt + k;
-            if (e < s.nstream) {
-                const uint64_t id = s.idx ? (uint64_t)__ldg(s.idx + e) : e;
-                if (id >= s.nverts) ok = false;  // index.rs:53 panics on this
-                vid[k] = (uint32_t)id;
+            for (int k = 0; k < 3; ++k) vid[k] = (uint32_t)(3 * lt + k);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint64_t e = 3 * lt + k;
+                if (e < s.nstream) {
+                    const uint64_t id = s.idx ? (uint64_t)__ldg(s.idx + e) : e;
+                    if (id >= s.nverts) ok = false;  // index.rs:53 panics on this
+                    vid[k] = (uint32_t)id;
+                }
             }
+            if (!ok) atomicCAS(err + si, 0, EUC_ERR_INDEX_OOB);
         }
-        if (!ok) atomicCAS(err + si, 0, EUC_ERR_INDEX_OOB);
+        const uint64_t cbase = s.geom ? s.gvtx_base : s.vtx_base;
         if (ok && lt < s.ntris) {
             float h[3][4], e3[3][3];
             const float flip1 = s.yflip ? -1.0f : 1.0f;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                const float4 c = clip[s.vtx_base + vid[k]];
+                const float4 c = clip[cbase + vid[k]];
                 h[k][0] = c.x * 1.0f;
                 h[k][1] = c.y * flip1;
                 h[k][2] = c.z;
@@ -1126,7 +1251,7 @@ EUC_DEV void resolve_direct_chunk(const SceneDev &s, const uint4 &cv, uint64_t l
         if (!s.pixel_write) continue;
         if constexpr (F::kDirect) {
             const typename F::U &u = *reinterpret_cast<const typename F::U *>(s.uniforms);
-            const float *vb = vdata + s.vd_base;
+            const float *vb = vdata + (s.geom ? s.gvd_base : s.vd_base);
             const TriRec &r = recs[t];
             float vd[F::NV], frag[F::NF];
             vdata_at<F>(s, r, vb, (float)x, (float)y, vd);
@@ -1220,7 +1345,7 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
 
     // 3. every thread evaluates jobs until the list is done
     const typename F::U &u = *reinterpret_cast<const typename F::U *>(s.uniforms);
-    const float *vb = vdata + s.vd_base;
+    const float *vb = vdata + (s.geom ? s.gvd_base : s.vd_base);
     const uint32_t L = s.level;
     for (uint32_t j = tid; j < njobs; j += kBlock) {
         const int slot = s_job[j] >> 2, c = s_job[j] & 3;
@@ -1473,7 +1598,7 @@ __global__ void __launch_bounds__(kBlock) k_resolve_ordered(const SceneDev *__re
     if (s.pixel_write)
         for (int i = 0; i < nch; ++i) ch[i] = pp[i];
     const typename F::U &u = *reinterpret_cast<const typename F::U *>(s.uniforms);
-    const float *vb = vdata + s.vd_base;
+    const float *vb = vdata + (s.geom ? s.gvd_base : s.vd_base);
     uint32_t last = 0;  // 1 + the primitive processed last
     for (uint32_t k = 0; k < n; ++k) {
         uint32_t best = 0xFFFFFFFFu, bz = 0;

@@ -135,7 +135,8 @@ class FrameSpec:
 
 def make_desc(shader, pixel_write=1, depth_test=abi.TEST_LESS, depth_write=1, y_axis=abi.Y_DOWN,
               z_clip=(0.0, 1.0), aa_level=0, cull=abi.CULL_BACK, blend=abi.BLEND_REPLACE,
-              band_rows=abi.BANDS_PAR, flags=0, handedness=abi.LEFT, primitives=abi.PRIM_TRIANGLE_LIST):
+              band_rows=abi.BANDS_PAR, flags=0, handedness=abi.LEFT, primitives=abi.PRIM_TRIANGLE_LIST,
+              geometry=abi.GEOM_NONE, geometry_param=0.0):
     """PipelineDesc with euc's defaults (CoordinateMode::VULKAN, CullMode::Back)."""
     d = abi.PipelineDesc()
     d.shader = shader
@@ -154,6 +155,8 @@ def make_desc(shader, pixel_write=1, depth_test=abi.TEST_LESS, depth_write=1, y_
     d.band_rows = band_rows
     d.flags = flags
     d.primitives = primitives
+    d.geometry = geometry
+    d.geometry_param = geometry_param
     return d
 
 

@@ -129,6 +129,21 @@ enum euc_primitives {
     EUC_PRIM_LINE_LIST = 2           /* LineList: lines 0-1, 2-3 (:79-104)                  */
 };
 
+/* Built-in geometry stages: `Pipeline::geometry` (pipeline.rs:221-229)
+ * turns each assembled triangle into 0..4 triangles, emitted in order
+ * (pipeline.rs:277-289).  New vertices are made the way a Rust geometry
+ * stage would with VertexData's Add/Mul: componentwise on the clip position
+ * and the vertex outputs.  TriangleList only.                              */
+enum euc_geometry {
+    EUC_GEOM_NONE = 0,      /* emit the triangle as it is (the default)                 */
+    EUC_GEOM_SUBDIVIDE = 1, /* 4 triangles on the edge midpoints p*0.5 + q*0.5:
+                               (a, ab, ca), (ab, b, bc), (ca, bc, c), (ab, bc, ca)        */
+    EUC_GEOM_SHRINK = 2,    /* each clip position pulled to the centroid
+                               m = ((a + b) + c) / 3: m + (v - m) * param                */
+    EUC_GEOM_DUPLICATE = 3, /* the triangle, then a copy with x += param * w           */
+    EUC_GEOM_DISCARD = 4    /* nothing when z / w > param at all three vertices         */
+};
+
 /* Mirrors the mode methods of `Pipeline` (pipeline.rs:178-209).            */
 typedef struct euc_pipeline_desc {
     uint32_t shader;      /* enum euc_shader                                  */
@@ -146,6 +161,8 @@ typedef struct euc_pipeline_desc {
     uint32_t band_rows;   /* EUC_BANDS_PAR, EUC_BANDS_SEQ or an explicit height */
     uint32_t flags;       /* EUC_FLAG_*                                       */
     uint32_t primitives;  /* enum euc_primitives (Pipeline::Primitives)       */
+    uint32_t geometry;    /* enum euc_geometry (Pipeline::geometry)           */
+    float geometry_param; /* parameter of the geometry stage                  */
 } euc_pipeline_desc;
 
 /* A 2-D target (Buffer2d, buffer.rs:183-219): row-major, y*pitch + x*bpp. */
@@ -372,7 +389,8 @@ int euc_sample_nearest(const void *texels, uint32_t ndim, const uint32_t *size, 
  * MiB per device that loads it, held until exit).  Limits: 65,536 vertices,
  * 65,536 primitives (index triples), 1,048,576 target pixels; larger scenes
  * return EUC_ERR_CAPACITY, and so do order-dependent blends (EUC_BLEND_ALPHA,
- * EUC_FLAG_ORDERED), whose fragment lists are sized on the device.  Runs on
+ * EUC_FLAG_ORDERED), whose fragment lists are sized on the device, and
+ * geometry stages, whose output vertices need room beyond the fixed array.  Runs on
  * the current device, ordered on `stream`.
  * `device_status` (nullable, device memory) receives EUC_OK or
  * EUC_ERR_INDEX_OOB once the render has run.  All calls share the scratch

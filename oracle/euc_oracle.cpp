@@ -729,6 +729,62 @@ struct Band {
 
 inline uint64_t read_index(const uint32_t *idx, uint64_t i) { return idx ? idx[i] : i; }
 
+// Built-in geometry stages (Pipeline::geometry, pipeline.rs:221-229, emitted
+// in order by pipeline.rs:277-289); the output triangles of each input
+// triangle, as documented with enum euc_geometry.  `c`: 3 clip positions,
+// `v`: 3 vertex outputs of nv floats.  Returns how many triangles it wrote
+// to oc / ov (up to 4).
+inline uint32_t geometry_ratio(uint32_t g) {
+    return g == EUC_GEOM_SUBDIVIDE ? 4u : g == EUC_GEOM_DUPLICATE ? 2u : 1u;
+}
+
+int geometry_stage(uint32_t g, float param, int nv, const float *c[3], const float *v[3], float *oc, float *ov) {
+    auto put = [&](int k, int j, const float *cc, const float *vv) {
+        for (int i = 0; i < 4; ++i) oc[(k * 3 + j) * 4 + i] = cc[i];
+        for (int i = 0; i < nv; ++i) ov[(k * 3 + j) * nv + i] = vv[i];
+    };
+    if (g == EUC_GEOM_SUBDIVIDE) {
+        std::vector<float> mc(3 * 4), mv(3 * (size_t)nv);
+        const int e[3][2] = {{0, 1}, {1, 2}, {2, 0}};  // ab, bc, ca
+        for (int m = 0; m < 3; ++m) {
+            for (int i = 0; i < 4; ++i) mc[m * 4 + i] = c[e[m][0]][i] * 0.5f + c[e[m][1]][i] * 0.5f;
+            for (int i = 0; i < nv; ++i) mv[m * nv + i] = v[e[m][0]][i] * 0.5f + v[e[m][1]][i] * 0.5f;
+        }
+        const float *ab = &mc[0], *bc = &mc[4], *ca = &mc[8];
+        const float *vab = &mv[0], *vbc = &mv[nv], *vca = &mv[2 * nv];
+        put(0, 0, c[0], v[0]); put(0, 1, ab, vab); put(0, 2, ca, vca);
+        put(1, 0, ab, vab); put(1, 1, c[1], v[1]); put(1, 2, bc, vbc);
+        put(2, 0, ca, vca); put(2, 1, bc, vbc); put(2, 2, c[2], v[2]);
+        put(3, 0, ab, vab); put(3, 1, bc, vbc); put(3, 2, ca, vca);
+        return 4;
+    }
+    if (g == EUC_GEOM_SHRINK) {
+        float m[4], s[4];
+        for (int i = 0; i < 4; ++i) m[i] = ((c[0][i] + c[1][i]) + c[2][i]) / 3.0f;
+        for (int j = 0; j < 3; ++j) {
+            for (int i = 0; i < 4; ++i) s[i] = m[i] + (c[j][i] - m[i]) * param;
+            put(0, j, s, v[j]);
+        }
+        return 1;
+    }
+    if (g == EUC_GEOM_DISCARD) {
+        bool beyond = true;
+        for (int j = 0; j < 3; ++j) beyond = beyond && (c[j][2] / c[j][3] > param);
+        if (beyond) return 0;
+    }
+    for (int j = 0; j < 3; ++j) put(0, j, c[j], v[j]);
+    if (g == EUC_GEOM_DUPLICATE) {
+        float s[4];
+        for (int j = 0; j < 3; ++j) {
+            for (int i = 0; i < 4; ++i) s[i] = c[j][i];
+            s[0] = c[j][0] + param * c[j][3];
+            put(1, j, s, v[j]);
+        }
+        return 2;
+    }
+    return 1;
+}
+
 template <class S>
 int render_impl(const S &sh, const euc_pipeline_desc &d, const void *verts, uint64_t nverts,
                 const euc_vertex_layout &lay, const uint32_t *idx, uint64_t nidx, const Target &pixel,
@@ -755,6 +811,23 @@ int render_impl(const S &sh, const euc_pipeline_desc &d, const void *verts, uint
     const uint8_t *vb = (const uint8_t *)verts;
     for (uint64_t i = 0; i < nshade; ++i)
         sh.vertex(vb + read_index(idx, i) * lay.stride, &clip[i * 4], &vout[i * S::NV]);
+    uint64_t nprim = ngroup;  // triangles (or line groups) handed to the rasteriser
+    if (d.geometry != EUC_GEOM_NONE) {  // triangles only (checked by the caller)
+        const uint32_t R = geometry_ratio(d.geometry);
+        std::vector<float> gclip(ngroup * R * 3 * 4), gvout(ngroup * R * 3 * (uint64_t)S::NV);
+        uint64_t out = 0;
+        for (uint64_t t = 0; t < ngroup; ++t) {
+            const float *c[3] = {&clip[(t * 3 + 0) * 4], &clip[(t * 3 + 1) * 4], &clip[(t * 3 + 2) * 4]};
+            const float *v[3] = {&vout[(t * 3 + 0) * S::NV], &vout[(t * 3 + 1) * S::NV], &vout[(t * 3 + 2) * S::NV]};
+            out += geometry_stage(d.geometry, d.geometry_param, S::NV, c, v, &gclip[out * 3 * 4],
+                                  &gvout[out * 3 * S::NV]);
+        }
+        gclip.resize(out * 3 * 4);
+        gvout.resize(out * 3 * S::NV);
+        clip.swap(gclip);
+        vout.swap(gvout);
+        nprim = out;
+    }
 
     const uint32_t level = d.aa_level > 6 ? 6 : d.aa_level;  // pipeline.rs:291-294
     // Row bands (pipeline.rs:328-345).
@@ -779,7 +852,7 @@ int render_impl(const S &sh, const euc_pipeline_desc &d, const void *verts, uint
             uint64_t r0 = b * gr, r1 = r0 + gr < size[1] ? r0 + gr : size[1];
             Band<S> band(sh, d, pixel, depth, size, r0, r1, level);
             if (d.primitives == EUC_PRIM_TRIANGLE_LIST) {
-                for (uint64_t t = 0; t < ngroup; ++t) {
+                for (uint64_t t = 0; t < nprim; ++t) {
                     const float *h[3] = {&clip[(t * 3 + 0) * 4], &clip[(t * 3 + 1) * 4], &clip[(t * 3 + 2) * 4]};
                     const float *o[3] = {&vout[(t * 3 + 0) * S::NV], &vout[(t * 3 + 1) * S::NV],
                                          &vout[(t * 3 + 2) * S::NV]};
@@ -835,7 +908,8 @@ int oracle_render(const euc_pipeline_desc *d, const void *uniforms, size_t usize
                   const void *verts, size_t nverts, const uint32_t *idx, size_t nidx, const euc_target *pixel,
                   const euc_target *depth, int threads, oracle_stats *st) {
     if (!d || !lay || !uniforms) return EUC_ERR_INVALID;
-    if (d->primitives > EUC_PRIM_LINE_LIST) return EUC_ERR_INVALID;
+    if (d->primitives > EUC_PRIM_LINE_LIST || d->geometry > EUC_GEOM_DISCARD) return EUC_ERR_INVALID;
+    if (d->geometry != EUC_GEOM_NONE && d->primitives != EUC_PRIM_TRIANGLE_LIST) return EUC_ERR_INVALID;
     if (nverts && !verts) return EUC_ERR_INVALID;
     Target px(pixel), dp(depth);
     if (d->pixel_write && px.data && fmt_bpp(px.fmt) == 0) return EUC_ERR_INVALID;

@@ -179,6 +179,15 @@ CASES = {
     "lines_ordered": (_lines(seed=40, flags=abi.FLAG_ORDERED), 0),
     "wireframe_bgra8": (lambda: scenes.wireframe_frame(seed=41), 0),
     "wireframe_msaa1_rgba8": (lambda: scenes.wireframe_frame(seed=42, fmt=abi.FMT_RGBA8, aa_level=1), 0),
+    # built-in geometry stages (Pipeline::geometry)
+    "geom_sphere_subdivide": (_mod(_sphere(seed=43), geometry=abi.GEOM_SUBDIVIDE), 0),
+    "geom_soup_shrink": (_soup(seed=44, geometry=abi.GEOM_SHRINK, geometry_param=0.6), 0),
+    "geom_soup_duplicate": (_soup(seed=45, geometry=abi.GEOM_DUPLICATE, geometry_param=0.05), 0),
+    "geom_soup_discard": (_soup(seed=46, geometry=abi.GEOM_DISCARD, geometry_param=0.5), 0),
+    "geom_knot_subdivide_aa1": (_mod(_knot(1, seed=47), geometry=abi.GEOM_SUBDIVIDE), 1),
+    "geom_tex_shrink": (_mod(_textured(abi.FILTER_LINEAR, abi.WRAP_TILE, seed=48), geometry=abi.GEOM_SHRINK,
+                             geometry_param=0.8), 0),
+    "geom_alpha_duplicate": (_soup(seed=49, alpha=True, geometry=abi.GEOM_DUPLICATE, geometry_param=-0.03), 0),
     "ordered_sphere": (_mod(_sphere(seed=3), flags=abi.FLAG_ORDERED), 0),
     "ordered_soup_less": (_soup(seed=1, flags=abi.FLAG_ORDERED), 0),
     "ordered_soup_equal": (_clear(_soup(seed=3, depth_test=abi.TEST_EQUAL, flags=abi.FLAG_ORDERED), "depth", 0.5), 0),

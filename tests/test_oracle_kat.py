@@ -197,3 +197,36 @@ def test_trailing_partial_primitive_is_dropped_but_its_index_is_checked():
     f = scenes.clip_triangles_frame(verts, [RED] * 4, 8, 8, indices=[0, 1, 2, 9])
     tg, _, rc = _render(f)
     assert rc == abi.ERR_INDEX_OOB and (tg["color"] == 0).all()  # the 4th index is fetched and panics
+
+
+# --- geometry stages (enum euc_geometry, Pipeline::geometry) -----------------
+def _geom_soup(geometry, param, **kw):
+    f = scenes.soup_frame(seed=5, width=96, height=64, ntris=300, area_hi=600.0)
+    f.passes[0].desc.geometry = geometry
+    f.passes[0].desc.geometry_param = param
+    for k, v in kw.items():
+        setattr(f.passes[0].desc, k, v)
+    return f
+
+
+def test_geometry_duplicate_in_place_changes_nothing_under_less():
+    # the copy (x += 0 * w) repeats every fragment; z == stored depth fails
+    # `Less`, so only the first copy draws (pipeline.rs:519-526)
+    ref = oracle.run_frame(_geom_soup(abi.GEOM_NONE, 0.0))[0]
+    dup = oracle.run_frame(_geom_soup(abi.GEOM_DUPLICATE, 0.0))[0]
+    assert np.array_equal(ref["color"], dup["color"]) and np.array_equal(ref["depth"], dup["depth"])
+
+
+def test_geometry_discard_all_or_nothing():
+    # soup z in [0.05, 0.95], w = 1: z / w > 2 never holds, z / w > -1 always does
+    ref = oracle.run_frame(_geom_soup(abi.GEOM_NONE, 0.0))[0]
+    keep = oracle.run_frame(_geom_soup(abi.GEOM_DISCARD, 2.0))[0]
+    gone = oracle.run_frame(_geom_soup(abi.GEOM_DISCARD, -1.0))[0]
+    assert np.array_equal(ref["color"], keep["color"])
+    assert (gone["color"] == 0).all() and (gone["depth"] == 1.0).all()
+
+
+def test_geometry_is_refused_for_lines():
+    f = scenes.lines_frame(seed=1, width=32, height=32, nlines=10)
+    f.passes[0].desc.geometry = abi.GEOM_SUBDIVIDE
+    assert oracle.run_frame(f)[2] == [abi.ERR_INVALID]
