@@ -86,15 +86,13 @@ def parse():
 
 
 def dist_env():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from euc_gb300 import replicas
+    return replicas.dist_env()
 
 
 def make_frames(args, rank):
-    from euc_gb300 import scenes
-    seed = args.seed + 1000 * rank
+    from euc_gb300 import replicas, scenes
+    seed = replicas.replica_seed(args.seed, rank)
     if args.workload == "sphere":
         return [scenes.sphere_frame(seed=seed + i) for i in range(args.scenes)]
     if args.workload == "soup":
@@ -279,7 +277,7 @@ def load_traffic():
 def run_gpu(args):
     import torch
     import torch.distributed as dist
-    from euc_gb300 import capi, frames as fr
+    from euc_gb300 import capi, replicas, frames as fr
 
     world, rank, local = dist_env()
     if world > 1:
@@ -347,12 +345,9 @@ def run_gpu(args):
             fn()
         e1.record(stream)
         torch.cuda.synchronize()
-        t = e0.elapsed_time(e1)
+        t = replicas.max_over_ranks(e0.elapsed_time(e1), device=dev)
         if world > 1:
-            tt = torch.tensor([t], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
             dist.barrier()
-            t = float(tt.item())
         return t
 
     # plain calls with per-stage CUDA events (the stage times of the roofline)

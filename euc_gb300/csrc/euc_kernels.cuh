@@ -437,6 +437,10 @@ EUC_DEV void setup_line(const SceneDev &s, int si, uint64_t lt, uint64_t t, cons
     cy1 = (uint32_t)wy2;
 }
 
+// Primitives whose full-row bbox holds at most this many pixels are walked
+// once in k_setup; when none of those pixels is inside, they get no rows.
+constexpr uint32_t kTinyPixels = 4;
+
 // ---------------------------------------------------------------------------
 // k_setup: triangles.rs:55-199, once per primitive (euc repeats it per band;
 // only the bbox clamp depends on the band and that is applied per row).
@@ -602,6 +606,26 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
 #pragma unroll
                 for (int k = 0; k < 8; ++k) dst[k] = src[k];
                 nrows = bx1 > bx0 ? by1 - by0 : 0u;
+                if (full_rows && (bx1 - bx0) * (by1 - by0) <= kTinyPixels) {
+                    // a tiny primitive: walk its few pixels here exactly as
+                    // k_raster would (full-bbox rows, triangles.rs:257-301);
+                    // one that covers none of them needs no raster work
+                    bool any = false;
+                    for (uint32_t y = by0; y < by1 && !any; ++y) {
+                        const float yf = (float)y, xsf = (float)bx0;
+                        float w0 = (o[0] + dyw[0] * yf) + dxw[0] * xsf;
+                        float w1 = (o[1] + dyw[1] * yf) + dxw[1] * xsf;
+                        float w2 = (o[2] + dyw[2] * yf) + dxw[2] * xsf;
+                        for (uint32_t x = bx0; x < bx1; ++x) {
+                            const float wu2 = (w2 - w0) - w1;
+                            any = any || (w0 >= 0.0f && w1 >= 0.0f && wu2 >= 0.0f);
+                            w0 = w0 + dxw[0];
+                            w1 = w1 + dxw[1];
+                            w2 = w2 + dxw[2];
+                        }
+                    }
+                    if (!any) nrows = 0;
+                }
                 if (nrows) {
                     cx0 = bx0;
                     cx1 = bx1;
