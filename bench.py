@@ -12,9 +12,10 @@ in HBM for `value`.
 Printed as one JSON line (rank 0):
   value        batched scenes/s through euc_render_batch (whole job)
   per_scene    scenes/s for the same scenes through euc_render one at a time
-  e2e          scenes/s through the blocking host-buffer call euc_render_host
-               (host->device copies of inputs and targets, device->host copy of
-               the targets, all inside the timed region)
+  e2e          scenes/s through the blocking host-buffer batch call
+               euc_render_host_batch (host->device copies of inputs and targets,
+               device->host copy of the targets, all inside the timed region);
+               per_scene_value: the same through euc_render_host per scene
   mfrag_per_s  candidate fragments (inside + z-clip, exact counts) per second
   roofline     algorithmic bytes per batch / the dominant stage's CUDA-event
                time per batch, against the measured HBM copy bandwidth
@@ -165,13 +166,14 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU legs (oracle = CPU restatement of euc's render_par)
 # ---------------------------------------------------------------------------
-def cpu_sample(frames, budget_s, start=0):
-    """Renders scenes start, start+1, ... with the oracle on every host thread
-    until `budget_s` has passed; returns (scenes, seconds, threads)."""
+def cpu_sample(frames, budget_s, start=0, cap=None):
+    """Renders scenes start, start+1, ... (rotating through `frames`) with the
+    oracle on every host thread until `budget_s` has passed, or `cap` scenes;
+    returns (scenes, seconds, threads)."""
     from oracle import oracle
     threads = oracle.hw_threads()
     n, t0 = 0, time.perf_counter()
-    while n < len(frames) and (time.perf_counter() - t0) < budget_s:
+    while (cap is None or n < cap) and (time.perf_counter() - t0) < budget_s:
         oracle.run_frame(frames[(start + n) % len(frames)], threads=threads)
         n += 1
     return n, time.perf_counter() - t0, threads
@@ -253,6 +255,72 @@ def run_e2e(ctx, frames, reps):
     for _ in range(reps):
         one_pass()
     return reps * len(frames) / (time.perf_counter() - t0)
+
+
+def run_e2e_batch(ctx, frames, reps):
+    """The batched form on host buffers (euc_render_host_batch): pass k of
+    every frame in the k-th call; inputs and targets go up, targets come
+    back, inside each timed call.  The host targets are reset to their clear
+    values before each step, outside the timed region."""
+    import ctypes as C
+    from euc_gb300 import abi
+    hosts = [f.alloc_host_targets() for f in frames]
+    clean = [{k: v.copy() for k, v in h.items()} for h in hosts]
+    npass = max(len(f.passes) for f in frames)
+    keep = []
+
+    def scene_arrays():
+        arrays = []
+        for k in range(npass):
+            sc = []
+            for f, h in zip(frames, hosts):
+                if k >= len(f.passes):
+                    continue
+                p = f.passes[k]
+                uni, kp = p.bind_uniforms(lambda src: f.host_texture_ptr(src, h))
+                keep.append((uni, kp))
+                s = abi.Scene()
+                s.desc = p.desc
+                s.layout = p.layout
+                s.vertices = p.vertices.ctypes.data
+                s.nverts = p.nverts
+                s.indices = p.indices.ctypes.data if p.indices is not None else None
+                s.nindices = p.indices.size if p.indices is not None else 0
+                pix = h[p.pixel] if p.pixel else None
+                dep = h[p.depth] if p.depth else None
+                fmt = f.target(p.pixel).fmt if p.pixel else abi.FMT_NONE
+                s.pixel = abi.Target(pix.ctypes.data, pix.shape[1], pix.shape[0], pix.strides[0], fmt) \
+                    if pix is not None else abi.Target(None, 0, 0, 0, 0)
+                s.depth = abi.Target(dep.ctypes.data, dep.shape[1], dep.shape[0], dep.strides[0], abi.FMT_R32F) \
+                    if dep is not None else abi.Target(None, 0, 0, 0, 0)
+                s.uniforms = C.addressof(uni)
+                s.uniforms_size = C.sizeof(uni)
+                sc.append(s)
+            arrays.append((abi.Scene * len(sc))(*sc))
+        return arrays
+
+    arrays = scene_arrays()
+
+    def reset():
+        for h, c in zip(hosts, clean):
+            for k in h:
+                np.copyto(h[k], c[k])
+
+    def step():
+        for arr in arrays:
+            rc = ctx.render_host_batch(arr)
+            if rc != abi.OK:
+                raise RuntimeError("euc_render_host_batch failed: %d" % rc)
+
+    reset()
+    step()  # warm-up (allocations, page-locked staging)
+    total = 0.0
+    for _ in range(reps):
+        reset()
+        t0 = time.perf_counter()
+        step()
+        total += time.perf_counter() - t0
+    return reps * len(frames) / total
 
 
 def load_peaks():
@@ -371,7 +439,7 @@ def run_gpu(args):
         batch.clear()
         for df in batch.frames:
             fr.render_frame(ctx, df, stream, clear=False)
-    per_scene = e2e = None
+    per_scene = e2e = e2e_per_scene = None
     if not args.only_batched:
         per_scene_pass()
         torch.cuda.synchronize()
@@ -383,7 +451,8 @@ def run_gpu(args):
         p1.record(stream)
         torch.cuda.synchronize()
         per_scene = args.scenes / (p0.elapsed_time(p1) / reps / 1e3)
-        e2e = run_e2e(ctx, specs, reps=1)
+        e2e = run_e2e_batch(ctx, specs, reps=max(2, min(args.steps, 5)))
+        e2e_per_scene = run_e2e(ctx, specs, reps=1)
     h2d, d2h = host_bytes(specs)
 
     alg_bytes = sum(f.algorithmic_bytes() for f in specs)
@@ -396,7 +465,8 @@ def run_gpu(args):
     if rank == 0 and not args.no_baseline and not args.only_batched:
         n, t, threads = cpu_sample(specs, args.cpu_seconds)
         cpu = {"value": n / t, "unit": WORKLOADS[args.workload][2], "cores": threads, "kind": "port",
-               "sample": "first %d of the %d scenes in %.1f s (oracle render_par, %d threads)" % (n, len(specs), t, threads)}
+               "sample": "%d scenes (rotating through the %d of one step) in %.1f s (oracle render_par, %d threads)"
+                         % (n, len(specs), t, threads)}
     if rank == 0:
         desc, _, unit = WORKLOADS[args.workload]
         out = {
@@ -426,7 +496,9 @@ def run_gpu(args):
             "pipeline_roofline": {"achieved": alg_bytes / (ms_step / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                                   "frac": alg_bytes / (ms_step / 1e3) / 1e9 / peak, "peak_kind": peak_kind},
             "e2e": {"value": e2e, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "path": "euc_render_host per scene (host buffers, blocking)"},
+                    "path": "euc_render_host_batch (host buffers, blocking; one call per pass)",
+                    "per_scene_value": e2e_per_scene,
+                    "per_scene_path": "euc_render_host per scene (host buffers, blocking)"},
             "cpu_baseline": cpu,
             "clocks": clk,
         }

@@ -27,6 +27,7 @@ SIGNATURES = {
                                   C.POINTER(abi.VertexLayout), C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
                                   C.POINTER(abi.Target), C.POINTER(abi.Target)]),
     "euc_render_batch": (C.c_int, [C.c_void_p, C.POINTER(abi.Scene), C.c_size_t, C.c_void_p]),
+    "euc_render_host_batch": (C.c_int, [C.c_void_p, C.POINTER(abi.Scene), C.c_size_t, C.c_int]),
     "euc_graph_create": (C.c_int, [C.c_void_p, C.POINTER(abi.Scene), C.c_size_t, C.POINTER(C.c_void_p)]),
     "euc_graph_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
     "euc_graph_destroy": (C.c_int, [C.c_void_p]),
@@ -162,6 +163,10 @@ class Context:
                                      C.byref(layout), vertices_ptr, nverts, indices_ptr, nindices,
                                      C.byref(pixel) if pixel is not None else None,
                                      C.byref(depth) if depth is not None else None)
+
+    def render_host_batch(self, arr, threads=0):
+        """euc_render_host_batch on a ctypes array of abi.Scene with host pointers."""
+        return lib().euc_render_host_batch(self.handle, arr, len(arr), threads)
 
     def render_batch(self, scenes, stream=None):
         arr = (abi.Scene * len(scenes))(*scenes)

@@ -9,6 +9,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
+#include <thread>
+#include <map>
+#include <atomic>
+#include <array>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -48,7 +53,9 @@ struct euc_ctx {
     int raster_blocks = 0;  // resident k_raster blocks per SM
     euc_tuning tune{};      // launch-shape overrides (0 = default)
     // buffers used by euc_render_host
-    DevBuf h_verts, h_idx, h_pixel, h_depth, h_tex[2];
+    DevBuf h_arena;    // host-buffer renders: inputs and targets on the device
+    DevBuf h_pinned;   // ... and their page-locked staging (cudaMallocHost)
+    DevBuf h_tex[1];   // texture ingest: staged host rows
     StageSlot slots[kStageSlots];
     int next_slot = 0;
     int last_nscenes = 0;
@@ -727,10 +734,10 @@ int euc_ctx_destroy(euc_ctx *ctx) {
     cudaDeviceSynchronize();
     DevBuf *bufs[] = {&ctx->clip, &ctx->vdata, &ctx->recs, &ctx->rows, &ctx->chunk_sums, &ctx->live_tri, &ctx->live_rowoff,
                       &ctx->totals, &ctx->vbuf, &ctx->err, &ctx->stats, &ctx->cov, &ctx->obsum, &ctx->frags,
-                      &ctx->h_verts,
-                      &ctx->h_idx, &ctx->h_pixel, &ctx->h_depth, &ctx->h_tex[0], &ctx->h_tex[1]};
+                      &ctx->plan, &ctx->galive, &ctx->h_arena, &ctx->h_tex[0]};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
+    if (ctx->h_pinned.p) cudaFreeHost(ctx->h_pinned.p);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     for (auto &s : ctx->slots) {
         if (s.host) cudaFreeHost(s.host);
@@ -1041,89 +1048,197 @@ int euc_sample_nearest(const void *texels, uint32_t ndim, const uint32_t *size, 
     return EUC_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Host-side copies for the host-buffer renders: the jobs are split into
+// 1 MiB pieces that `threads` host threads take in turn (0: the hardware
+// concurrency, at most 16); small totals stay on the calling thread.
+struct CopyJob {
+    void *dst;
+    const void *src;
+    size_t bytes;
+};
+
+void parallel_copy(const std::vector<CopyJob> &jobs, int threads) {
+    constexpr size_t kPiece = 1u << 20;
+    size_t total = 0;
+    for (const CopyJob &j : jobs) total += j.bytes;
+    if (threads <= 0) {
+        const unsigned hc = std::thread::hardware_concurrency();
+        threads = hc ? (int)std::min(hc, 16u) : 1;
+    }
+    if (threads <= 1 || total < 4 * kPiece) {
+        for (const CopyJob &j : jobs)
+            if (j.bytes) std::memcpy(j.dst, j.src, j.bytes);
+        return;
+    }
+    std::vector<CopyJob> pieces;
+    for (const CopyJob &j : jobs)
+        for (size_t o = 0; o < j.bytes; o += kPiece)
+            pieces.push_back({(char *)j.dst + o, (const char *)j.src + o, std::min(kPiece, j.bytes - o)});
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+        for (size_t i; (i = next.fetch_add(1)) < pieces.size();) std::memcpy(pieces[i].dst, pieces[i].src, pieces[i].bytes);
+    };
+    std::vector<std::thread> pool;
+    const size_t nt = std::min<size_t>((size_t)threads, pieces.size());
+    for (size_t t = 1; t < nt; ++t) {
+        try {
+            pool.emplace_back(work);
+        } catch (...) {
+            break;  // fewer helpers; the calling thread still finishes every piece
+        }
+    }
+    work();
+    for (std::thread &th : pool) th.join();
+}
+
+// Scenes whose vertex, index, texture (inside the uniforms) and target
+// pointers are host memory: every input is staged into page-locked memory,
+// moved with one copy, rendered as one batch, and the targets come back with
+// one copy.  Nothing is written back when a scene fails.
+int host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int threads) {
+    struct Region {
+        const void *src;
+        size_t bytes, off;
+    };
+    struct alignas(16) UniBuf {
+        unsigned char b[512];
+        unsigned char *data() { return b; }
+    };
+    std::vector<euc_scene> dev(scenes, scenes + n);
+    std::vector<UniBuf> unis(n);
+    std::vector<Region> in, out;
+    std::vector<size_t> voff(n, SIZE_MAX), ioff(n, SIZE_MAX), poff(n, SIZE_MAX), doff(n, SIZE_MAX);
+    std::vector<std::array<size_t, 2>> toff(n, {SIZE_MAX, SIZE_MAX});
+    std::map<const void *, size_t> shared_tex;
+    size_t off = 0;
+    auto place = [&](std::vector<Region> &list, const void *src, size_t bytes) {
+        const size_t at = off;
+        list.push_back({src, bytes, at});
+        off = pad_up(off + bytes, 256);
+        return at;
+    };
+    static_assert(sizeof(euc_phong_uniforms) <= 512, "uniform copies hold any shader's struct");
+    for (size_t i = 0; i < n; ++i) {
+        const euc_scene &sc = scenes[i];
+        Plan p;
+        if (int rc = plan_scene(sc, p)) return rc;
+        const size_t need = uniforms_size_for(sc.desc.shader);
+        std::memcpy(unis[i].data(), sc.uniforms, need);
+        dev[i].uniforms = unis[i].data();
+        dev[i].uniforms_size = need;
+        if (p.skip) continue;
+        const size_t vb = (size_t)sc.nverts * sc.layout.stride;
+        if (vb) voff[i] = place(in, sc.vertices, vb);
+        if (sc.indices && sc.nindices) ioff[i] = place(in, sc.indices, (size_t)sc.nindices * 4);
+        euc_sampler *samp[2] = {nullptr, nullptr};
+        if (sc.desc.shader == EUC_SHADER_TEXTURED) samp[0] = &((euc_textured_uniforms *)unis[i].data())->tex;
+        if (sc.desc.shader == EUC_SHADER_PHONG) {
+            samp[0] = &((euc_phong_uniforms *)unis[i].data())->tex;
+            samp[1] = &((euc_phong_uniforms *)unis[i].data())->shadow;
+        }
+        for (int k = 0; k < 2; ++k) {
+            if (!samp[k] || !samp[k]->data) continue;
+            const size_t pitch = samp[k]->pitch ? samp[k]->pitch : (size_t)samp[k]->width * 4;
+            const size_t bytes = pitch * samp[k]->height;
+            auto it = shared_tex.find(samp[k]->data);
+            toff[i][k] = it != shared_tex.end() ? it->second : (shared_tex[samp[k]->data] = place(in, samp[k]->data, bytes));
+        }
+    }
+    const size_t targets_at = off;  // targets last: one copy back covers them all
+    for (size_t i = 0; i < n; ++i) {
+        const euc_scene &sc = scenes[i];
+        if (sc.pixel.data) {
+            const uint32_t bpp = fmt_bpp(sc.pixel.format);
+            if (!bpp) return EUC_ERR_INVALID;
+            const size_t pitch = sc.pixel.pitch ? sc.pixel.pitch : (size_t)sc.pixel.width * bpp;
+            poff[i] = place(out, sc.pixel.data, pitch * sc.pixel.height);
+        }
+        if (sc.depth.data) {
+            const size_t pitch = sc.depth.pitch ? sc.depth.pitch : (size_t)sc.depth.width * 4;
+            doff[i] = place(out, sc.depth.data, pitch * sc.depth.height);
+        }
+    }
+    const size_t total = std::max<size_t>(off, 256);
+    int rc;
+    if ((rc = grow(ctx->h_arena, total))) return rc;
+    if (ctx->h_pinned.cap < total) {
+        if (ctx->h_pinned.p) CUDA_TRY(cudaFreeHost(ctx->h_pinned.p));
+        ctx->h_pinned.p = nullptr;
+        ctx->h_pinned.cap = 0;
+        CUDA_TRY(cudaMallocHost(&ctx->h_pinned.p, total));
+        ctx->h_pinned.cap = total;
+    }
+    unsigned char *d = (unsigned char *)ctx->h_arena.p, *h = (unsigned char *)ctx->h_pinned.p;
+    for (size_t i = 0; i < n; ++i) {
+        if (voff[i] != SIZE_MAX) dev[i].vertices = d + voff[i];
+        if (ioff[i] != SIZE_MAX) dev[i].indices = (const uint32_t *)(d + ioff[i]);
+        if (poff[i] != SIZE_MAX) dev[i].pixel.data = d + poff[i];
+        if (doff[i] != SIZE_MAX) dev[i].depth.data = d + doff[i];
+        for (int k = 0; k < 2; ++k) {
+            if (toff[i][k] == SIZE_MAX) continue;
+            euc_sampler *smp = k == 0 ? (dev[i].desc.shader == EUC_SHADER_TEXTURED
+                                             ? &((euc_textured_uniforms *)unis[i].data())->tex
+                                             : &((euc_phong_uniforms *)unis[i].data())->tex)
+                                      : &((euc_phong_uniforms *)unis[i].data())->shadow;
+            smp->data = d + toff[i][k];
+        }
+    }
+    std::vector<CopyJob> jobs;
+    for (const Region &r : in) jobs.push_back({h + r.off, r.src, r.bytes});
+    for (const Region &r : out) jobs.push_back({h + r.off, r.src, r.bytes});
+    parallel_copy(jobs, threads);
+    CUDA_TRY(cudaMemcpyAsync(d, h, off, cudaMemcpyHostToDevice, nullptr));
+    if ((rc = run_batch(ctx, dev.data(), n, nullptr))) return rc;
+    if (off > targets_at)
+        CUDA_TRY(cudaMemcpyAsync(h + targets_at, d + targets_at, off - targets_at, cudaMemcpyDeviceToHost, nullptr));
+    CUDA_TRY(cudaStreamSynchronize(nullptr));
+    // device-side errors (index out of bounds): nothing is written back
+    if (ctx->last_nscenes) {
+        std::vector<int> e(ctx->last_nscenes);
+        CUDA_TRY(cudaMemcpy(e.data(), ctx->err.p, e.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        for (int v : e)
+            if (v) return v;
+    }
+    jobs.clear();
+    for (const Region &r : out) jobs.push_back({const_cast<void *>(r.src), h + r.off, r.bytes});
+    parallel_copy(jobs, threads);
+    return EUC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int euc_render_host(euc_ctx *ctx, const euc_pipeline_desc *desc, const void *uniforms, size_t uniforms_size,
                     const euc_vertex_layout *layout, const void *vertices, size_t nverts, const uint32_t *indices,
                     size_t nindices, const euc_target *pixel, const euc_target *depth) {
     if (!ctx || !desc || !layout || !uniforms) return EUC_ERR_INVALID;
-    const size_t need = uniforms_size_for(desc->shader);
-    if (need == 0 || uniforms_size < need) return EUC_ERR_INVALID;
-    std::unique_lock<std::mutex> g(ctx->mu);
-    CUDA_TRY(cudaSetDevice(ctx->device));
-    int rc;
-    // vertices, indices
-    const size_t vbytes = nverts * layout->stride;
-    if ((rc = grow(ctx->h_verts, std::max<size_t>(vbytes, 4)))) return rc;
-    if (vbytes) CUDA_TRY(cudaMemcpy(ctx->h_verts.p, vertices, vbytes, cudaMemcpyHostToDevice));
-    const uint32_t *didx = nullptr;
-    if (indices) {
-        if ((rc = grow(ctx->h_idx, std::max<size_t>(nindices * 4, 4)))) return rc;
-        if (nindices) CUDA_TRY(cudaMemcpy(ctx->h_idx.p, indices, nindices * 4, cudaMemcpyHostToDevice));
-        didx = (const uint32_t *)ctx->h_idx.p;
-    }
-    // textures: host pointers inside the uniforms become device copies
-    alignas(16) unsigned char ubuf[sizeof(euc_phong_uniforms) + 64];
-    std::memcpy(ubuf, uniforms, need);
-    euc_sampler *samp[2] = {nullptr, nullptr};
-    if (desc->shader == EUC_SHADER_TEXTURED) samp[0] = &((euc_textured_uniforms *)ubuf)->tex;
-    if (desc->shader == EUC_SHADER_PHONG) {
-        samp[0] = &((euc_phong_uniforms *)ubuf)->tex;
-        samp[1] = &((euc_phong_uniforms *)ubuf)->shadow;
-    }
-    for (int k = 0; k < 2; ++k) {
-        if (!samp[k] || !samp[k]->data) continue;
-        if ((rc = check_sampler(*samp[k]))) return rc;
-        const size_t pitch = samp[k]->pitch ? samp[k]->pitch : (size_t)samp[k]->width * 4;
-        const size_t bytes = pitch * samp[k]->height;
-        if ((rc = grow(ctx->h_tex[k], bytes))) return rc;
-        CUDA_TRY(cudaMemcpy(ctx->h_tex[k].p, samp[k]->data, bytes, cudaMemcpyHostToDevice));
-        samp[k]->data = ctx->h_tex[k].p;
-    }
-    // targets
-    euc_target tp = pixel ? *pixel : euc_target{nullptr, 0, 0, 0, EUC_FMT_NONE};
-    euc_target td = depth ? *depth : euc_target{nullptr, 0, 0, 0, EUC_FMT_NONE};
-    void *hp = tp.data, *hd = td.data;
-    size_t pbytes = 0, dbytes = 0;
-    if (hp) {
-        const uint32_t bpp = fmt_bpp(tp.format);
-        if (!bpp) return EUC_ERR_INVALID;
-        const size_t pitch = tp.pitch ? tp.pitch : (size_t)tp.width * bpp;
-        pbytes = pitch * tp.height;
-        if ((rc = grow(ctx->h_pixel, std::max<size_t>(pbytes, 4)))) return rc;
-        CUDA_TRY(cudaMemcpy(ctx->h_pixel.p, hp, pbytes, cudaMemcpyHostToDevice));
-        tp.data = ctx->h_pixel.p;
-    }
-    if (hd) {
-        const size_t pitch = td.pitch ? td.pitch : (size_t)td.width * 4;
-        dbytes = pitch * td.height;
-        if ((rc = grow(ctx->h_depth, std::max<size_t>(dbytes, 4)))) return rc;
-        CUDA_TRY(cudaMemcpy(ctx->h_depth.p, hd, dbytes, cudaMemcpyHostToDevice));
-        td.data = ctx->h_depth.p;
-    }
-    euc_scene s;
-    std::memset(&s, 0, sizeof(s));
-    s.desc = *desc;
-    s.layout = *layout;
-    s.vertices = ctx->h_verts.p;
-    s.nverts = nverts;
-    s.indices = didx;
-    s.nindices = nindices;
-    s.pixel = tp;
-    s.depth = td;
-    s.uniforms = ubuf;
-    s.uniforms_size = need;
-    if ((rc = run_batch(ctx, &s, 1, nullptr))) return rc;
-    CUDA_TRY(cudaStreamSynchronize(nullptr));
-    // device-side errors (index out of bounds) leave the targets untouched
-    if (ctx->last_nscenes) {
-        int e = 0;
-        CUDA_TRY(cudaMemcpy(&e, ctx->err.p, sizeof(int), cudaMemcpyDeviceToHost));
-        if (e) return e;
-    }
-    if (hp) CUDA_TRY(cudaMemcpy(hp, ctx->h_pixel.p, pbytes, cudaMemcpyDeviceToHost));
-    if (hd) CUDA_TRY(cudaMemcpy(hd, ctx->h_depth.p, dbytes, cudaMemcpyDeviceToHost));
-    return EUC_OK;
+    euc_scene sc;
+    std::memset(&sc, 0, sizeof(sc));
+    sc.desc = *desc;
+    sc.layout = *layout;
+    sc.vertices = vertices;
+    sc.nverts = nverts;
+    sc.indices = indices;
+    sc.nindices = indices ? nindices : 0;
+    if (pixel) sc.pixel = *pixel;
+    if (depth) sc.depth = *depth;
+    sc.uniforms = uniforms;
+    sc.uniforms_size = uniforms_size;
+    return euc_render_host_batch(ctx, &sc, 1, 0);
 }
 
+int euc_render_host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int threads) {
+    if (!ctx || (n && !scenes)) return EUC_ERR_INVALID;
+    if (!n) return EUC_OK;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CUDA_TRY(cudaSetDevice(ctx->device));
+    return host_batch(ctx, scenes, n, threads);
+}
 }  // extern "C"
 
 // ===========================================================================

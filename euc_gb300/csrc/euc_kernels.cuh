@@ -911,6 +911,31 @@ EUC_DEV void raster_row(const SceneDev &s, const TriRec &r, uint32_t t, uint32_t
     const bool kmin = s.keytype == KEY_MIN, greater = s.depth_test == EUC_TEST_GREATER;
     const uint32_t tmin = (t + 1u) << 1;
     const unsigned long long tlast = (unsigned long long)(~t) << 32;
+    if (kmin && !probe) {
+        // Less / Greater with depth writes, fire-and-forget reductions: each
+        // candidate is keyed and reduced where the walk finds it
+        const uint32_t flip = greater ? 0xFFFFFFFFu : 0u;
+#pragma unroll 4
+        for (uint32_t x = xs; x < xe; ++x) {
+            const float wu2 = (w2 - w0) - w1;
+            if (w0 >= 0.0f && w1 >= 0.0f && wu2 >= 0.0f) {
+                const float z = (z0 * w0 + z1 * w1) + z2 * wu2;
+                if (noclip || (s.zmin <= z && z <= s.zmax)) {
+                    ++cnt;
+                    if (z == z) {  // a NaN depth fails every test (partial_cmp is None)
+                        const uint32_t b = __float_as_uint(z + 0.0f);  // -0 and +0 compare equal
+                        const uint32_t o = (b ^ ((uint32_t)((int32_t)b >> 31) | 0x80000000u)) ^ flip;
+                        const uint32_t neg0 = __float_as_uint(z) == 0x80000000u ? 1u : 0u;
+                        atomicMin(row_keys + x, ((unsigned long long)o << 32) | (tmin | neg0));
+                    }
+                }
+            }
+            w0 = w0 + d0;
+            w1 = w1 + d1;
+            w2 = w2 + d2;
+        }
+        return;
+    }
     // The walk advances pixel by pixel exactly as euc's loop does; candidates
     // are gathered kWalk at a time so that their key loads are in flight
     // together instead of one L2 round trip per pixel.

@@ -335,6 +335,16 @@ int euc_render_host(euc_ctx *ctx, const euc_pipeline_desc *desc, const void *uni
                     size_t nverts, const uint32_t *indices, size_t nindices,
                     const euc_target *pixel, const euc_target *depth);
 
+/* Batched form on host buffers (blocking): every scene's vertex, index,
+ * texture (in its uniforms) and target pointers are host memory, as for
+ * euc_render_host.  Inputs are staged into page-locked memory by `threads`
+ * host threads (0: the hardware concurrency, at most 16) and moved with one
+ * copy; the batch renders as euc_render_batch; the targets come back with
+ * one copy.  If any scene fails, no target is written back.  Textures that
+ * several scenes share (the same host pointer) are copied once.  No
+ * counterpart in euc.                                                       */
+int euc_render_host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int threads);
+
 /* Batched form: renders `n` independent scenes with one set of launches
  * (grouped by shader kind).  Each output is byte-identical to the scene
  * rendered alone with euc_render.  No counterpart in euc.                   */
