@@ -363,7 +363,7 @@ def run_gpu(args):
     tuning, tune_info = None, None
     if not args.no_tune:
         from euc_gb300 import autotune
-        tuning, tune_info = autotune.tune(ctx, batch, stream)
+        tuning, tune_info = autotune.tune(ctx, batch, stream, reps=9)
     # the recorded form of the same batch (scenes on the ordered path cannot be recorded)
     graph = None
     if not args.no_graph and not any(s.desc.blend == 1 or s.desc.flags & 2 for arr in batch.scene_arrays()

@@ -289,7 +289,7 @@ int plan_scene(const euc_scene &sc, Plan &p) {
     // fragment: those scenes (and any with EUC_FLAG_ORDERED) replay per-pixel
     // fragment lists instead of reducing visibility keys
     if ((s.pixel_write && d.blend == EUC_BLEND_ALPHA) || (d.flags & EUC_FLAG_ORDERED)) s.keytype = KEY_ORDERED;
-    p.nv = (uint32_t)shader_nv(d.shader);
+    p.nv = (uint32_t)vd_stride(shader_nv(d.shader));  // padded VertexData floats per vertex
     p.uniforms = sc.uniforms;
     p.usize = need;
     return EUC_OK;
@@ -504,7 +504,7 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
         p.d.pix_base = pix;
         res_base[i] = res;
         vtx += pad_up(p.d.nverts, kBlock);
-        vd += p.d.nverts * p.nv;
+        vd += pad_up(p.d.nverts * p.nv, 4);  // 16-byte aligned regions: vector gathers
         tri += pad_up(std::max<uint64_t>(p.d.ngroups, 1), kBlock);
         pix += pad_up((uint64_t)p.d.W * p.d.H, kBlock);
         res += resolve_blocks(p.d);
@@ -522,7 +522,7 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
         p.d.gvtx_base = vtx;
         p.d.gvd_base = vd;
         vtx += 3ull * p.d.ntris;
-        vd += 3ull * p.d.ntris * p.nv;
+        vd += pad_up(3ull * p.d.ntris * p.nv, 4);
     }
     if (tri >= 0x7FFFFFF0ull) return EUC_ERR_CAPACITY;  // visibility keys hold a 31-bit primitive id
     const uint64_t nchunks = tri / kBlock;
@@ -756,7 +756,7 @@ int euc_ctx_reserve(euc_ctx *ctx, uint64_t max_verts, uint64_t max_tris, uint64_
     const uint64_t vtx = max_verts + ns * kBlock, tri = max_tris + ns * kBlock, pix = max_pixels + ns * kBlock;
     int rc;
     if ((rc = grow(ctx->clip, vtx * sizeof(float4)))) return rc;
-    if ((rc = grow(ctx->vdata, vtx * 11 * sizeof(float)))) return rc;
+    if ((rc = grow(ctx->vdata, (vtx * vd_stride(11) + 4 * ns) * sizeof(float)))) return rc;
     if ((rc = grow(ctx->recs, tri * sizeof(TriRec)))) return rc;
     if ((rc = grow(ctx->rows, tri * sizeof(uint32_t)))) return rc;
     if ((rc = grow(ctx->chunk_sums, (tri / kBlock + 1) * sizeof(uint2)))) return rc;
@@ -1251,7 +1251,7 @@ int euc_render_host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int t
 // whole device.  An euc_ctx grows its scratch buffers on demand, so such a
 // caller cannot use euc_render.  This entry point takes the same inputs and
 // outputs but keeps all of its scratch in one fixed array of this file,
-// g_noalloc_scratch (kNaBytes, about 20.8 MiB).  Every GPU that loads this
+// g_noalloc_scratch (kNaBytes, about 21.0 MiB).  Every GPU that loads this
 // library holds that array until the process exits.
 //
 // Limits: at most kNaMaxVerts vertices, kNaMaxGroups primitives (index
@@ -1273,7 +1273,7 @@ namespace {
 constexpr uint64_t kNaMaxVerts = 65536;
 constexpr uint64_t kNaMaxGroups = 65536;
 constexpr uint64_t kNaMaxPixels = 1ull << 20;
-constexpr int kNaMaxNV = 11;  // PhongFn::NV, the largest VertexData
+constexpr int kNaMaxNV = vd_stride(11);  // PhongFn::NV, the largest VertexData, padded
 constexpr size_t kNaStage = 4096;  // scene table, bases, uniforms
 constexpr size_t kNaOffErr = kNaStage;
 constexpr size_t kNaOffStats = kNaOffErr + 256;

@@ -38,6 +38,45 @@ constexpr int kBlock = 256;           // threads per block in every kernel
 constexpr int kScanPer = 8;           // primitives per thread in k_scan
 constexpr int kScanBlock = kBlock * kScanPer;
 
+// VertexData floats per vertex in vdata[]: more than four are padded to a
+// multiple of four, so that their gathers in the resolve are 16-byte loads;
+// up to four are stored as they are (padding three to four costs more in
+// traffic than it saves in loads).
+__host__ __device__ constexpr int vd_stride(int nv) { return nv <= 4 ? nv : (nv + 3) & ~3; }
+
+template <class F>
+EUC_DEV void load_vd(const float *__restrict__ p, float out[vd_stride(F::NV)]) {
+    constexpr int S = vd_stride(F::NV);
+    if constexpr (S % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < S; i += 4) {
+            const float4 q = __ldg(reinterpret_cast<const float4 *>(p + i));
+            out[i] = q.x;
+            out[i + 1] = q.y;
+            out[i + 2] = q.z;
+            out[i + 3] = q.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < S; ++i) out[i] = p[i];
+    }
+}
+
+template <class F>
+EUC_DEV void store_vd(float *__restrict__ p, const float *v) {
+    constexpr int S = vd_stride(F::NV);
+    if constexpr (S % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < S; i += 4)
+            *reinterpret_cast<float4 *>(p + i) = make_float4(i < F::NV ? v[i] : 0.0f, i + 1 < F::NV ? v[i + 1] : 0.0f,
+                                                             i + 2 < F::NV ? v[i + 2] : 0.0f,
+                                                             i + 3 < F::NV ? v[i + 3] : 0.0f);
+    } else {
+#pragma unroll
+        for (int i = 0; i < S; ++i) p[i] = v[i];
+    }
+}
+
 // KEY_MIN / KEY_LAST: order-independent visibility keys (see above).
 // KEY_ORDERED: every candidate fragment is kept in a per-pixel list and the
 // lists are replayed in submission order (blends that read the old pixel).
@@ -181,9 +220,7 @@ __global__ void __launch_bounds__(kBlock) k_vertex(const SceneDev *__restrict__ 
     float c[4], vd[F::NV];
     F::vertex(u, s.lay, s.verts + v * s.lay.stride, c, vd);
     clip[s.vtx_base + v] = make_float4(c[0], c[1], c[2], c[3]);
-    float *out = vdata + s.vd_base + v * F::NV;
-#pragma unroll
-    for (int i = 0; i < F::NV; ++i) out[i] = vd[i];
+    store_vd<F>(vdata + s.vd_base + v * vd_stride(F::NV), vd);
 }
 
 // ---------------------------------------------------------------------------
@@ -275,7 +312,7 @@ __global__ void __launch_bounds__(kBlock) k_geometry(const SceneDev *__restrict_
         for (int j = 0; j < 3; ++j) {
             const float4 q = clip[s.vtx_base + vid[j]];
             c[j][0] = q.x; c[j][1] = q.y; c[j][2] = q.z; c[j][3] = q.w;
-            const float *src = vdata + s.vd_base + (uint64_t)vid[j] * F::NV;
+            const float *src = vdata + s.vd_base + (uint64_t)vid[j] * vd_stride(F::NV);
 #pragma unroll
             for (int i = 0; i < F::NV; ++i) v[j][i] = src[i];
         }
@@ -289,9 +326,7 @@ __global__ void __launch_bounds__(kBlock) k_geometry(const SceneDev *__restrict_
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
             clip[s.gvtx_base + o + j] = make_float4(oc[j][0], oc[j][1], oc[j][2], oc[j][3]);
-            float *dst = vdata + s.gvd_base + (o + j) * F::NV;
-#pragma unroll
-            for (int i = 0; i < F::NV; ++i) dst[i] = ov[j][i];
+            store_vd<F>(vdata + s.gvd_base + (o + j) * vd_stride(F::NV), ov[j]);
         }
     }
 }
@@ -859,15 +894,11 @@ EUC_DEV void raster_line_step(const SceneDev &s, const TriRec &r, uint32_t t, ui
     if (!probe || kv < __ldcg(key)) atomicMin(key, kv);
 }
 
-EUC_DEV void raster_row(const SceneDev &s, const TriRec &r, uint32_t t, uint32_t y,
-                        unsigned long long *__restrict__ vbuf, uint32_t &cnt, int phase, uint2 *__restrict__ frags,
-                        bool probe) {
-    if (s.prim != EUC_PRIM_TRIANGLE_LIST) {  // lines: `y` is the step within the window
-        raster_line_step(s, r, t, y, vbuf, cnt, phase, frags, probe);
-        return;
-    }
+// The pixel span [xs, xe) of row y of triangle r: the whole band-clamped
+// bbox row when the extent is below 128, else the edge intersections
+// (triangles.rs:219-253).  False when it is empty.
+EUC_DEV bool row_span(const SceneDev &s, const TriRec &r, uint32_t y, uint32_t &xs, uint32_t &xe) {
     const float yf = (float)y;
-    uint32_t xs, xe;
     bool full = r.flags & 2u;  // one band, extent < 128 (k_setup)
     if (!full) {
         // band of this row and the band-clamped bbox (pipeline.rs:341-360, triangles.rs:114-139)
@@ -897,8 +928,20 @@ EUC_DEV void raster_row(const SceneDev &s, const TriRec &r, uint32_t t, uint32_t
         xs = (fl >= fx0 && fl < fx1) ? sat_u32(fl) : r.bx0;
         xe = (ce >= fx0 && ce < fx1) ? sat_u32(ce) : r.bx1;
     }
-    if (xs >= xe) return;
+    return xs < xe;
+}
+
+EUC_DEV void raster_row(const SceneDev &s, const TriRec &r, uint32_t t, uint32_t y,
+                        unsigned long long *__restrict__ vbuf, uint32_t &cnt, int phase, uint2 *__restrict__ frags,
+                        bool probe) {
+    if (s.prim != EUC_PRIM_TRIANGLE_LIST) {  // lines: `y` is the step within the window
+        raster_line_step(s, r, t, y, vbuf, cnt, phase, frags, probe);
+        return;
+    }
+    uint32_t xs, xe;
+    if (!row_span(s, r, y, xs, xe)) return;
     // row-start weights, then the serial walk (triangles.rs:257-301)
+    const float yf = (float)y;
     const float xsf = (float)xs;
     float w0 = (r.o[0] + r.dy[0] * yf) + r.dx[0] * xsf;
     float w1 = (r.o[1] + r.dy[1] * yf) + r.dx[1] * xsf;
@@ -1127,14 +1170,19 @@ EUC_DEV void get_v_data(const TriRec &r, const float *__restrict__ vd0, const fl
 template <class F>
 EUC_DEV void vdata_at(const SceneDev &s, const TriRec &r, const float *__restrict__ vb, float xf, float yf,
                       float *out) {
-    const float *v0 = vb + (uint64_t)r.v[0] * F::NV, *v1 = vb + (uint64_t)r.v[1] * F::NV;
+    constexpr int S = vd_stride(F::NV);
+    float a0[S], a1[S];
+    load_vd<F>(vb + (uint64_t)r.v[0] * S, a0);
+    load_vd<F>(vb + (uint64_t)r.v[1] * S, a1);
     if (s.prim != EUC_PRIM_TRIANGLE_LIST) {
         const float frac = ((r.flags & kLineUseX) ? xf - r.o[0] : yf - r.o[1]) * r.o[2];
 #pragma unroll
-        for (int i = 0; i < F::NV; ++i) out[i] = v0[i] * (1.0f - frac) + v1[i] * frac;
+        for (int i = 0; i < F::NV; ++i) out[i] = a0[i] * (1.0f - frac) + a1[i] * frac;
         return;
     }
-    get_v_data<F>(r, v0, v1, vb + (uint64_t)r.v[2] * F::NV, xf, yf, out);
+    float a2[S];
+    load_vd<F>(vb + (uint64_t)r.v[2] * S, a2);
+    get_v_data<F>(r, a0, a1, a2, xf, yf, out);
 }
 
 // Decodes a visibility key; false when no fragment passed at this pixel.

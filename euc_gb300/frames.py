@@ -244,7 +244,15 @@ class BatchGraph:
 
     def __init__(self, ctx, batch):
         self.batch = batch
-        self.graphs = [ctx.graph(arr) for arr in batch.scene_arrays()]
+        arrays = batch.scene_arrays()
+        self.graphs = [ctx.graph(arr) for arr in arrays]
+        if len(arrays) > 1:
+            # recording a later pass may have grown the context scratch that
+            # an earlier pass was recorded against: record again, now that the
+            # scratch holds every pass
+            for g in self.graphs:
+                g.close()
+            self.graphs = [ctx.graph(arr) for arr in arrays]
 
     def launch(self, stream=None, clear=True):
         if clear:

@@ -395,7 +395,7 @@ int euc_sample_nearest(const void *texels, uint32_t ndim, const uint32_t *size, 
  * euc: it exists for callers that may not allocate device memory, such as an
  * engine or plugin host that owns a fixed device-memory budget, or a render
  * thread that cannot pay for cudaMalloc/cudaFree (both synchronise the whole
- * device).  Scratch lives in one fixed array inside the library (about 20.8
+ * device).  Scratch lives in one fixed array inside the library (about 21.0
  * MiB per device that loads it, held until exit).  Limits: 65,536 vertices,
  * 65,536 primitives (index triples), 1,048,576 target pixels; larger scenes
  * return EUC_ERR_CAPACITY, and so do order-dependent blends (EUC_BLEND_ALPHA,

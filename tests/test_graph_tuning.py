@@ -57,6 +57,24 @@ def test_graph_replays_are_byte_identical(which):
         ctx.close()
 
 
+def test_two_pass_graph_on_a_fresh_context():
+    """Recording pass 1 grows the scratch that pass 0 was recorded against;
+    BatchGraph records again so that every pass replays."""
+    import torch
+    specs = _knot()
+    ctx = capi.Context(0)
+    try:
+        batch = fr.DeviceBatch(specs, "cuda:0")
+        g = fr.BatchGraph(ctx, batch)  # before any render on this context
+        g.launch()
+        torch.cuda.synchronize()
+        got = (batch.color.clone(), batch.depth.clone())
+        g.close()
+        assert _same(got, _render(ctx, batch))
+    finally:
+        ctx.close()
+
+
 def test_graph_sees_new_buffer_contents():
     """The graph holds pointers, not contents: new vertex data in the same
     buffers renders as a plain batch of the new data does."""
