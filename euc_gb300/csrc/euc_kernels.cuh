@@ -780,7 +780,7 @@ constexpr int kChunkGroup = 16;
 // kBlock apart, so that every load and store instruction of a warp covers 32
 // consecutive entries and the kInitPer depth loads are in flight together; a
 // chunk is kBlock * kInitPer entries.
-constexpr int kInitPer = 4;
+constexpr int kInitPer = 8;
 constexpr int kInitChunk = kBlock * kInitPer;
 
 // Scene of chunk `c` given the scene of an earlier chunk of the same group.
@@ -1212,11 +1212,15 @@ EUC_DEV void store_pixel(const SceneDev &s, uint32_t x, uint32_t y, const float 
         reinterpret_cast<uint32_t *>(p)[x] = r8 | (g8 << 8) | (b8 << 16) | (a8 << 24);
     } else if (s.pfmt == EUC_FMT_BGRA8) {
         reinterpret_cast<uint32_t *>(p)[x] = b8 | (g8 << 8) | (r8 << 16) | (a8 << 24);
-    } else {
+    } else {  // RGB8: two stores, the 2-byte one on its even address
         p += 3ull * x;
-        p[0] = (uint8_t)r8;
-        p[1] = (uint8_t)g8;
-        p[2] = (uint8_t)b8;
+        if (((uintptr_t)p & 1u) == 0) {
+            *reinterpret_cast<uint16_t *>(p) = (uint16_t)(r8 | (g8 << 8));
+            p[2] = (uint8_t)b8;
+        } else {
+            p[0] = (uint8_t)r8;
+            *reinterpret_cast<uint16_t *>(p + 1) = (uint16_t)(g8 | (b8 << 8));
+        }
     }
 }
 
