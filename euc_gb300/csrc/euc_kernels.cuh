@@ -1118,14 +1118,26 @@ __global__ void __launch_bounds__(kBlock, 4) k_raster(const SceneDev *__restrict
         for (int j = lane; j < witems; j += 32) off[j] = l0 + j < nlive ? live_rowoff[l0 + j] : ~0ull;
         __syncwarp();
         uint32_t scene0 = 0xFFFFFFFFu, cnt0 = 0;
+        // The 32 items of a step are consecutive, so their primitives are a
+        // run of the window from a0 (the primitive of the step's first item):
+        // lane j marks where primitive a0 + 1 + j starts within the step, and
+        // each lane counts the starts at or before its own item.
+        int a0 = 0;  // window entry 0 is the primitive of item `base`
         for (int s = 0; s < witems / 32; ++s) {
-            const uint64_t i = base + (uint64_t)s * 32 + lane;
-            if (i >= nitems) break;
-            int a = 0, b = witems;  // the last window entry that starts at or before i
-            while (b - a > 1) {
-                const int mid = (a + b) >> 1;
-                if (off[mid] <= i) a = mid; else b = mid;
+            const uint64_t i0 = base + (uint64_t)s * 32;
+            if (i0 >= nitems) break;
+            const int c = a0 + 1 + lane;
+            uint32_t bit = 0;
+            if (lane < 31 && c < witems) {
+                const uint64_t o = off[c];
+                if (o > i0 && o < i0 + 32) bit = 1u << (uint32_t)(o - i0);
             }
+            const uint32_t starts = __reduce_or_sync(0xFFFFFFFFu, bit);
+            const int a = a0 + __popc(starts & ((2u << lane) - 1u));
+            const int alast = a0 + __popc(starts);  // the primitive of the step's last item
+            a0 = (alast + 1 < witems && off[alast + 1] == i0 + 32) ? alast + 1 : alast;
+            const uint64_t i = i0 + lane;
+            if (i >= nitems) continue;
             const uint32_t t = live_tri[l0 + a];
             const TriRec &r = recs[t];
             const uint32_t scene = r.scene;
