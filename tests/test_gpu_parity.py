@@ -120,6 +120,18 @@ def _unindexed():
     return make
 
 
+def _ragged(nverts, prims=abi.PRIM_TRIANGLE_LIST, indexed=False):
+    """A stream of `nverts` vertices: empty, or shorter than one primitive."""
+    def make():
+        rng = np.random.default_rng(nverts)
+        clip = np.concatenate([rng.uniform(-0.9, 0.9, (nverts, 2)), rng.uniform(0.1, 0.9, (nverts, 1)),
+                               np.ones((nverts, 1))], axis=1)
+        col = np.full((nverts, 4), 200, dtype=np.uint8)
+        idx = np.arange(nverts, dtype=np.uint32)[::-1].copy() if indexed else None
+        return scenes.clip_triangles_frame(clip, col, 32, 24, indices=idx, primitives=prims)
+    return make
+
+
 def _lines(seed=31, prims=abi.PRIM_LINE_LIST, **kw):
     return lambda: scenes.lines_frame(seed=seed, prims=prims, **kw)
 
@@ -166,6 +178,13 @@ CASES = {
     "alpha_soup_rgb8": (_fmt(_soup(seed=26, alpha=True), abi.FMT_RGB8), 0),
     "alpha_soup_bgra8": (_fmt(_soup(seed=27, alpha=True), abi.FMT_BGRA8), 0),
     # replace blends forced through the ordered path must give the same bytes
+    # empty and ragged streams: nothing is drawn (primitives.rs collect_primitive)
+    "empty_stream": (_ragged(0), 0),
+    "empty_indexed": (_ragged(0, indexed=True), 0),
+    "two_vertices": (_ragged(2), 0),
+    "five_vertices_indexed": (_ragged(5, indexed=True), 0),
+    "one_vertex_lines": (_ragged(1, prims=abi.PRIM_LINE_LIST), 0),
+    "five_vertices_line_tris": (_ragged(5, prims=abi.PRIM_LINE_TRIANGLE_LIST), 0),
     # lines (lines.rs) and the wireframe example's LineTriangleList pipeline
     "lines_less": (_lines(), 0),
     "lines_tri_list": (_lines(seed=32, prims=abi.PRIM_LINE_TRIANGLE_LIST, nlines=2000), 0),
