@@ -454,6 +454,9 @@ def run_gpu(args):
         e2e = run_e2e_batch(ctx, specs, reps=max(2, min(args.steps, 5)))
         e2e_per_scene = run_e2e(ctx, specs, reps=1)
     h2d, d2h = host_bytes(specs)
+    host_copy = ("in place: kernels read vertices and indices and update targets in host memory over "
+                 "NVLink-C2C; one kernel gathers the textures") if ctx.host_copy_direct() else \
+        "staged through page-locked memory by host threads, one copy each way"
 
     alg_bytes = sum(f.algorithmic_bytes() for f in specs)
     dom = max(stage_ms, key=lambda k: stage_ms[k])
@@ -497,6 +500,9 @@ def run_gpu(args):
                                   "frac": alg_bytes / (ms_step / 1e3) / 1e9 / peak, "peak_kind": peak_kind},
             "e2e": {"value": e2e, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "path": "euc_render_host_batch (host buffers, blocking; one call per pass)",
+                    "host_copy": host_copy,
+                    "bytes": "host-buffer bytes each step's calls read (inputs, textures, targets) and write "
+                             "(targets); in place, only the covered pixels of a target cross the link",
                     "per_scene_value": e2e_per_scene,
                     "per_scene_path": "euc_render_host per scene (host buffers, blocking)"},
             "cpu_baseline": cpu,

@@ -34,6 +34,7 @@ TEST_NONE, TEST_LESS, TEST_EQUAL, TEST_GREATER = 0, 1, 2, 3
 PRIM_TRIANGLE_LIST, PRIM_LINE_TRIANGLE_LIST, PRIM_LINE_LIST = 0, 1, 2
 SRC_RGBA8, SRC_BGRA8, SRC_RGB8, SRC_LUMA8, SRC_LUMA_ALPHA8, SRC_R32F = 0, 1, 2, 3, 4, 5
 GEOM_NONE, GEOM_SUBDIVIDE, GEOM_SHRINK, GEOM_DUPLICATE, GEOM_DISCARD = 0, 1, 2, 3, 4
+HOST_COPY_AUTO, HOST_COPY_STAGED, HOST_COPY_DIRECT = 0, 1, 2
 CULL_NONE, CULL_BACK, CULL_FRONT = 0, 1, 2
 Y_DOWN, Y_UP = 0, 1
 LEFT, RIGHT = 0, 1
@@ -123,7 +124,8 @@ class Stats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("raster_blocks_per_sm", C.c_uint32), ("raster_warp_rows", C.c_uint32),
-                ("chunk_group", C.c_uint32), ("chunk_blocks_per_sm", C.c_uint32), ("raster_probe", C.c_uint32)]
+                ("chunk_group", C.c_uint32), ("chunk_blocks_per_sm", C.c_uint32), ("raster_probe", C.c_uint32),
+                ("host_copy", C.c_uint32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

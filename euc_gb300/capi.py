@@ -141,6 +141,18 @@ class Context:
         check(lib().euc_ctx_get_tuning(self.handle, C.byref(t)), "euc_ctx_get_tuning")
         return t
 
+    def host_copy_direct(self):
+        """True when host-buffer renders use their buffers in place (the
+        device reads pageable host memory and host_copy is not STAGED)."""
+        t = self.get_tuning()
+        if t.host_copy == abi.HOST_COPY_STAGED:
+            return False
+        probe = abi.Tuning(**t.as_dict())
+        probe.host_copy = abi.HOST_COPY_DIRECT
+        ok = lib().euc_ctx_set_tuning(self.handle, C.byref(probe)) == abi.OK
+        self.set_tuning(t)
+        return ok
+
     def set_profiling(self, on):
         check(lib().euc_ctx_set_profiling(self.handle, 1 if on else 0), "euc_ctx_set_profiling")
 

@@ -51,6 +51,7 @@ struct euc_ctx {
     DevBuf plan;          // k_plan: k_init and k_resolve chunk bases (2 x (scenes + 1))
     DevBuf galive;        // geometry stage: 1 per output slot that holds a triangle
     int raster_blocks = 0;  // resident k_raster blocks per SM
+    bool pageable = false;  // kernels may access pageable host memory (cudaDevAttrPageableMemoryAccess)
     euc_tuning tune{};      // launch-shape overrides (0 = default)
     // buffers used by euc_render_host
     DevBuf h_arena;    // host-buffer renders: inputs and targets on the device
@@ -720,10 +721,13 @@ int euc_ctx_create(int device, euc_ctx **out) {
     if (!c) return EUC_ERR_OOM;
     c->device = device;
     c->raster_blocks = raster_blocks_per_sm();
-    if (cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
         delete c;
         return EUC_ERR_CUDA;
     }
+    c->pageable = pageable != 0;
     *out = c;
     return EUC_OK;
 }
@@ -779,6 +783,8 @@ int euc_ctx_set_tuning(euc_ctx *ctx, const euc_tuning *t) {
         if (v.raster_warp_rows && (v.raster_warp_rows % 32 || v.raster_warp_rows > (uint32_t)kWarpItems))
             return EUC_ERR_INVALID;
         if (v.raster_blocks_per_sm > 64 || v.chunk_group > 1024 || v.chunk_blocks_per_sm > 64 || v.raster_probe > 2)
+            return EUC_ERR_INVALID;
+        if (v.host_copy > EUC_HOST_COPY_DIRECT || (v.host_copy == EUC_HOST_COPY_DIRECT && !ctx->pageable))
             return EUC_ERR_INVALID;
     }
     std::lock_guard<std::mutex> g(ctx->mu);
@@ -1095,10 +1101,34 @@ void parallel_copy(const std::vector<CopyJob> &jobs, int threads) {
     for (std::thread &th : pool) th.join();
 }
 
+// Sampler k (0: the texture, 1: Phong's shadow map) in a scene's copy of its
+// uniforms.
+euc_sampler *sampler_of(const euc_scene &sc, unsigned char *uni, int k) {
+    if (k == 0)
+        return sc.desc.shader == EUC_SHADER_TEXTURED ? &((euc_textured_uniforms *)uni)->tex
+                                                     : &((euc_phong_uniforms *)uni)->tex;
+    return &((euc_phong_uniforms *)uni)->shadow;
+}
+
+// The first device-side error (an index out of bounds) of the last batch,
+// after its stream has been synchronised.
+int first_scene_error(euc_ctx *ctx) {
+    if (!ctx->last_nscenes) return EUC_OK;
+    std::vector<int> e(ctx->last_nscenes);
+    CUDA_TRY(cudaMemcpy(e.data(), ctx->err.p, e.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int v : e)
+        if (v) return v;
+    return EUC_OK;
+}
+
 // Scenes whose vertex, index, texture (inside the uniforms) and target
-// pointers are host memory: every input is staged into page-locked memory,
-// moved with one copy, rendered as one batch, and the targets come back with
-// one copy.  Nothing is written back when a scene fails.
+// pointers are host memory, rendered as one batch.  On a device that reads
+// pageable host memory, the kernels use the vertices, indices and targets
+// where they lie, and one k_copy_pieces launch gathers the textures (sampled
+// many times each) into a device arena.  Elsewhere, host threads stage every
+// input and target into page-locked memory, one copy moves each direction,
+// and the targets are copied back.  A scene that fails draws nothing; the
+// others are drawn, as in euc_render_batch.
 int host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int threads) {
     struct Region {
         const void *src;
@@ -1122,6 +1152,7 @@ int host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int threads) {
         return at;
     };
     static_assert(sizeof(euc_phong_uniforms) <= 512, "uniform copies hold any shader's struct");
+    const bool direct = ctx->pageable && ctx->tune.host_copy != EUC_HOST_COPY_STAGED;
     for (size_t i = 0; i < n; ++i) {
         const euc_scene &sc = scenes[i];
         Plan p;
@@ -1132,24 +1163,20 @@ int host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int threads) {
         dev[i].uniforms_size = need;
         if (p.skip) continue;
         const size_t vb = (size_t)sc.nverts * sc.layout.stride;
-        if (vb) voff[i] = place(in, sc.vertices, vb);
-        if (sc.indices && sc.nindices) ioff[i] = place(in, sc.indices, (size_t)sc.nindices * 4);
-        euc_sampler *samp[2] = {nullptr, nullptr};
-        if (sc.desc.shader == EUC_SHADER_TEXTURED) samp[0] = &((euc_textured_uniforms *)unis[i].data())->tex;
-        if (sc.desc.shader == EUC_SHADER_PHONG) {
-            samp[0] = &((euc_phong_uniforms *)unis[i].data())->tex;
-            samp[1] = &((euc_phong_uniforms *)unis[i].data())->shadow;
-        }
-        for (int k = 0; k < 2; ++k) {
-            if (!samp[k] || !samp[k]->data) continue;
-            const size_t pitch = samp[k]->pitch ? samp[k]->pitch : (size_t)samp[k]->width * 4;
-            const size_t bytes = pitch * samp[k]->height;
-            auto it = shared_tex.find(samp[k]->data);
-            toff[i][k] = it != shared_tex.end() ? it->second : (shared_tex[samp[k]->data] = place(in, samp[k]->data, bytes));
+        if (vb && !direct) voff[i] = place(in, sc.vertices, vb);
+        if (sc.indices && sc.nindices && !direct) ioff[i] = place(in, sc.indices, (size_t)sc.nindices * 4);
+        const int nsamp = sc.desc.shader == EUC_SHADER_PHONG ? 2 : sc.desc.shader == EUC_SHADER_TEXTURED ? 1 : 0;
+        for (int k = 0; k < nsamp; ++k) {
+            const euc_sampler *smp = sampler_of(sc, unis[i].data(), k);
+            if (!smp->data) continue;
+            const size_t pitch = smp->pitch ? smp->pitch : (size_t)smp->width * 4;
+            const size_t bytes = pitch * smp->height;
+            auto it = shared_tex.find(smp->data);
+            toff[i][k] = it != shared_tex.end() ? it->second : (shared_tex[smp->data] = place(in, smp->data, bytes));
         }
     }
     const size_t targets_at = off;  // targets last: one copy back covers them all
-    for (size_t i = 0; i < n; ++i) {
+    for (size_t i = 0; i < n && !direct; ++i) {
         const euc_scene &sc = scenes[i];
         if (sc.pixel.data) {
             const uint32_t bpp = fmt_bpp(sc.pixel.format);
@@ -1162,9 +1189,38 @@ int host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int threads) {
             doff[i] = place(out, sc.depth.data, pitch * sc.depth.height);
         }
     }
-    const size_t total = std::max<size_t>(off, 256);
+    // direct: the texture piece table follows the regions
+    constexpr size_t kPiece = 128u << 10;
+    std::vector<CopyPiece> pieces;
+    size_t tab = 0, total = std::max<size_t>(off, 256);
+    if (direct) {
+        for (const Region &r : in)
+            for (size_t o = 0; o < r.bytes; o += kPiece)
+                pieces.push_back({(const uint8_t *)r.src + o, nullptr, std::min(kPiece, r.bytes - o)});
+        tab = pad_up(off, 256);
+        total = tab + pieces.size() * sizeof(CopyPiece) + 256;
+    }
     int rc;
     if ((rc = grow(ctx->h_arena, total))) return rc;
+    if (direct) {
+        unsigned char *d = (unsigned char *)ctx->h_arena.p;
+        size_t k = 0;
+        for (const Region &r : in)
+            for (size_t o = 0; o < r.bytes; o += kPiece) pieces[k++].dst = d + r.off + o;
+        for (size_t i = 0; i < n; ++i)
+            for (int t = 0; t < 2; ++t)
+                if (toff[i][t] != SIZE_MAX) sampler_of(dev[i], unis[i].data(), t)->data = d + toff[i][t];
+        if (!pieces.empty()) {
+            CUDA_TRY(cudaMemcpyAsync(d + tab, pieces.data(), pieces.size() * sizeof(CopyPiece), cudaMemcpyHostToDevice,
+                                     nullptr));
+            k_copy_pieces<<<(unsigned)pieces.size(), kBlock, 0, nullptr>>>((const CopyPiece *)(d + tab));
+            CUDA_TRY(cudaGetLastError());
+            ctx->launches += 1;
+        }
+        if ((rc = run_batch(ctx, dev.data(), n, nullptr))) return rc;
+        CUDA_TRY(cudaStreamSynchronize(nullptr));
+        return first_scene_error(ctx);
+    }
     if (ctx->h_pinned.cap < total) {
         if (ctx->h_pinned.p) CUDA_TRY(cudaFreeHost(ctx->h_pinned.p));
         ctx->h_pinned.p = nullptr;
@@ -1178,14 +1234,8 @@ int host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int threads) {
         if (ioff[i] != SIZE_MAX) dev[i].indices = (const uint32_t *)(d + ioff[i]);
         if (poff[i] != SIZE_MAX) dev[i].pixel.data = d + poff[i];
         if (doff[i] != SIZE_MAX) dev[i].depth.data = d + doff[i];
-        for (int k = 0; k < 2; ++k) {
-            if (toff[i][k] == SIZE_MAX) continue;
-            euc_sampler *smp = k == 0 ? (dev[i].desc.shader == EUC_SHADER_TEXTURED
-                                             ? &((euc_textured_uniforms *)unis[i].data())->tex
-                                             : &((euc_phong_uniforms *)unis[i].data())->tex)
-                                      : &((euc_phong_uniforms *)unis[i].data())->shadow;
-            smp->data = d + toff[i][k];
-        }
+        for (int t = 0; t < 2; ++t)
+            if (toff[i][t] != SIZE_MAX) sampler_of(dev[i], unis[i].data(), t)->data = d + toff[i][t];
     }
     std::vector<CopyJob> jobs;
     for (const Region &r : in) jobs.push_back({h + r.off, r.src, r.bytes});
@@ -1196,17 +1246,12 @@ int host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int threads) {
     if (off > targets_at)
         CUDA_TRY(cudaMemcpyAsync(h + targets_at, d + targets_at, off - targets_at, cudaMemcpyDeviceToHost, nullptr));
     CUDA_TRY(cudaStreamSynchronize(nullptr));
-    // device-side errors (index out of bounds): nothing is written back
-    if (ctx->last_nscenes) {
-        std::vector<int> e(ctx->last_nscenes);
-        CUDA_TRY(cudaMemcpy(e.data(), ctx->err.p, e.size() * sizeof(int), cudaMemcpyDeviceToHost));
-        for (int v : e)
-            if (v) return v;
-    }
+    // a scene that failed on the device drew nothing: its targets come back
+    // as they went up
     jobs.clear();
     for (const Region &r : out) jobs.push_back({const_cast<void *>(r.src), h + r.off, r.bytes});
     parallel_copy(jobs, threads);
-    return EUC_OK;
+    return first_scene_error(ctx);
 }
 
 }  // namespace

@@ -1536,6 +1536,44 @@ __global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__
 }
 
 // ---------------------------------------------------------------------------
+// Host-buffer renders on a device that reads pageable host memory: one block
+// per piece of a region, 16-byte words with four loads in flight per thread
+// (the link's latency is microseconds), 4-byte or single-byte words where
+// the piece's ends are not aligned that far.
+// ---------------------------------------------------------------------------
+struct CopyPiece {
+    const uint8_t *src;
+    uint8_t *dst;
+    uint64_t bytes;
+};
+
+__global__ void __launch_bounds__(kBlock) k_copy_pieces(const CopyPiece *__restrict__ pieces) {
+    const CopyPiece p = pieces[blockIdx.x];
+    const uint64_t n = p.bytes;
+    const uintptr_t al = (uintptr_t)p.src | (uintptr_t)p.dst | (uintptr_t)n;
+    if ((al & 15) == 0) {
+        const uint4 *s = (const uint4 *)p.src;
+        uint4 *d = (uint4 *)p.dst;
+        const uint64_t n16 = n / 16;
+        uint64_t i = threadIdx.x;
+        for (; i + 3 * kBlock < n16; i += 4 * kBlock) {
+            const uint4 a = s[i], b = s[i + kBlock], c = s[i + 2 * kBlock], e = s[i + 3 * kBlock];
+            d[i] = a;
+            d[i + kBlock] = b;
+            d[i + 2 * kBlock] = c;
+            d[i + 3 * kBlock] = e;
+        }
+        for (; i < n16; i += kBlock) d[i] = s[i];
+    } else if ((al & 3) == 0) {
+        const uint32_t *s = (const uint32_t *)p.src;
+        uint32_t *d = (uint32_t *)p.dst;
+        for (uint64_t i = threadIdx.x; i < n / 4; i += kBlock) d[i] = s[i];
+    } else {
+        for (uint64_t i = threadIdx.x; i < n; i += kBlock) p.dst[i] = p.src[i];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Texture ingest: one thread per texel, image-crate layouts -> sampler layouts.
 // ---------------------------------------------------------------------------
 __host__ __device__ inline uint32_t src_bpp(uint32_t f) {

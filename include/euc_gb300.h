@@ -302,7 +302,17 @@ typedef struct euc_tuning {
     uint32_t chunk_group;          /* 256-pixel chunks per scene lookup in init/resolve (adaptive)   */
     uint32_t chunk_blocks_per_sm;  /* init/resolve grid cap per SM (16)                              */
     uint32_t raster_probe;         /* 1: read a key before its atomicMin, 2: atomics only (default)  */
+    uint32_t host_copy;            /* host-buffer renders: EUC_HOST_COPY_* (AUTO)                    */
 } euc_tuning;
+
+/* How euc_render_host / euc_render_host_batch reach host buffers.  DIRECT
+ * has the kernels use the vertices, indices and targets in host memory and
+ * gathers only the textures; it needs a device that accesses pageable host
+ * memory coherently (cudaDevAttrPageableMemoryAccess, e.g. over
+ * NVLink-C2C), and euc_ctx_set_tuning refuses it elsewhere.  STAGED copies
+ * everything through page-locked memory with host threads.  AUTO takes
+ * DIRECT where it can.                                                      */
+enum euc_host_copy { EUC_HOST_COPY_AUTO = 0, EUC_HOST_COPY_STAGED = 1, EUC_HOST_COPY_DIRECT = 2 };
 int euc_ctx_set_tuning(euc_ctx *ctx, const euc_tuning *tuning);
 int euc_ctx_get_tuning(euc_ctx *ctx, euc_tuning *tuning);
 
@@ -326,10 +336,11 @@ int euc_render(euc_ctx *ctx, const euc_pipeline_desc *desc, const void *uniforms
                size_t nverts, const uint32_t *indices, size_t nindices, const euc_target *pixel,
                const euc_target *depth, void *stream);
 
-/* The same render on HOST buffers, blocking, like the Rust call: copies the
- * vertices, indices, textures and targets to the device, renders, copies the
- * targets back and returns the final status.  Texture pointers inside the
- * uniforms are host pointers here.                                          */
+/* The same render on HOST buffers, blocking, like the Rust call; it returns
+ * the final status.  Texture pointers inside the uniforms are host pointers
+ * here.  The buffers reach the device as euc_tuning.host_copy says: in
+ * place where the device reads pageable host memory (textures gathered),
+ * else copied through page-locked memory and the targets copied back.      */
 int euc_render_host(euc_ctx *ctx, const euc_pipeline_desc *desc, const void *uniforms,
                     size_t uniforms_size, const euc_vertex_layout *layout, const void *vertices,
                     size_t nverts, const uint32_t *indices, size_t nindices,
@@ -337,10 +348,14 @@ int euc_render_host(euc_ctx *ctx, const euc_pipeline_desc *desc, const void *uni
 
 /* Batched form on host buffers (blocking): every scene's vertex, index,
  * texture (in its uniforms) and target pointers are host memory, as for
- * euc_render_host.  Inputs are staged into page-locked memory by `threads`
- * host threads (0: the hardware concurrency, at most 16) and moved with one
- * copy; the batch renders as euc_render_batch; the targets come back with
- * one copy.  If any scene fails, no target is written back.  Textures that
+ * euc_render_host, and the batch renders as euc_render_batch.  Under
+ * EUC_HOST_COPY_DIRECT the kernels read the vertices and indices and update
+ * the targets where they lie in host memory; only the textures are gathered
+ * into device memory, by one kernel.  Under EUC_HOST_COPY_STAGED `threads`
+ * host threads (0: the hardware concurrency, at most 16) stage every input
+ * and target into page-locked memory, one copy moves each direction, and
+ * the targets are copied back.  A scene that fails draws nothing and the
+ * others are drawn; the first failure's status is returned.  Textures that
  * several scenes share (the same host pointer) are copied once.  No
  * counterpart in euc.                                                       */
 int euc_render_host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int threads);

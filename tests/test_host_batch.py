@@ -1,5 +1,7 @@
 """euc_render_host_batch (host buffers, one call per pass) against the
-oracle and against euc_render_host per scene: byte-identical targets."""
+oracle and against euc_render_host per scene: byte-identical targets, under either way of
+moving host buffers (page-locked staging, or kernels that read and write
+host memory directly)."""
 import ctypes as C
 
 import numpy as np
@@ -33,8 +35,22 @@ def _host_scene(f, p, h, keep):
     return s
 
 
-def _render_host_batch(ctx, frames, threads):
-    hosts = [f.alloc_host_targets() for f in frames]
+def _context(host_copy):
+    """A context whose host-buffer renders use `host_copy`; skips where the
+    device cannot read pageable host memory and DIRECT is asked for."""
+    ctx = capi.Context(0)
+    t = abi.Tuning()
+    t.host_copy = host_copy
+    rc = capi.lib().euc_ctx_set_tuning(ctx.handle, C.byref(t))
+    if rc == abi.ERR_INVALID and host_copy == abi.HOST_COPY_DIRECT:
+        ctx.close()
+        pytest.skip("the device does not access pageable host memory")
+    assert rc == abi.OK
+    return ctx
+
+
+def _render_host_batch(ctx, frames, threads, hosts=None):
+    hosts = hosts or [f.alloc_host_targets() for f in frames]
     keep = []
     for k in range(max(len(f.passes) for f in frames)):
         sc = [_host_scene(f, f.passes[k], h, keep) for f, h in zip(frames, hosts) if k < len(f.passes)]
@@ -43,13 +59,14 @@ def _render_host_batch(ctx, frames, threads):
     return hosts
 
 
-@pytest.mark.parametrize("threads", [1, 0])
-def test_host_batch_matches_oracle(threads):
+@pytest.mark.parametrize("threads,host_copy", [(1, abi.HOST_COPY_STAGED), (0, abi.HOST_COPY_STAGED),
+                                               (0, abi.HOST_COPY_AUTO), (0, abi.HOST_COPY_DIRECT)])
+def test_host_batch_matches_oracle(threads, host_copy):
     frames = scenes.batch_frames(seed=17, n=10, tri_lo=50, tri_hi=20000, resolutions=(64, 128, 200), tex_size=32)
     frames += [scenes.knot_frame(seed=3, width=160, height=96, shadow_size=128, tubular=120, radial=16, tex_size=32),
                scenes.sphere_frame(seed=9, width=97, height=61, lon=24, lat=12),
                scenes.lines_frame(seed=2, width=128, height=80, nlines=500)]
-    ctx = capi.Context(0)
+    ctx = _context(host_copy)
     try:
         got = _render_host_batch(ctx, frames, threads)
     finally:
@@ -61,18 +78,88 @@ def test_host_batch_matches_oracle(threads):
         assert_targets_match(f, ref, g, color_tol=tol)
 
 
-def test_host_batch_writes_nothing_back_on_failure():
+@pytest.mark.parametrize("host_copy", [abi.HOST_COPY_STAGED, abi.HOST_COPY_DIRECT])
+def test_host_batch_unaligned_targets(host_copy):
+    """RGB8 targets at odd host addresses with odd row lengths: the copies
+    fall back to narrower words and still land byte for byte."""
+    frames = [scenes.sphere_frame(seed=s, width=w, height=h, lon=16, lat=8)
+              for s, (w, h) in enumerate([(97, 61), (33, 17), (64, 48)])]
+    ctx = _context(host_copy)
+    try:
+        ref = _render_host_batch(ctx, frames, 0)
+        odd = []
+        for f in frames:
+            h = f.alloc_host_targets()
+            c = h["color"]
+            raw = np.zeros(c.size + 1, dtype=np.uint8)
+            view = raw[1:].reshape(c.shape)
+            view[...] = c
+            h["color"] = view
+            odd.append(h)
+        got = _render_host_batch(ctx, frames, 0, hosts=odd)
+    finally:
+        ctx.close()
+    for r, g in zip(ref, got):
+        assert g["color"].ctypes.data % 2 == 1
+        for k in r:
+            assert np.array_equal(r[k].view(np.uint8), g[k].view(np.uint8)), k
+
+
+@pytest.mark.parametrize("host_copy", [abi.HOST_COPY_STAGED, abi.HOST_COPY_DIRECT])
+def test_host_batch_failing_scene_draws_nothing(host_copy):
+    """A scene with an index out of bounds leaves its targets as they were;
+    the other scene of the batch is drawn as it is alone (euc_render_batch's
+    rule)."""
     good = scenes.sphere_frame(seed=1, width=64, height=48, lon=12, lat=6)
     bad = scenes.sphere_frame(seed=2, width=64, height=48, lon=12, lat=6)
     bad.passes[0].indices = bad.passes[0].indices.copy()
     bad.passes[0].indices[4] = 100000
-    ctx = capi.Context(0)
+    ctx = _context(host_copy)
     try:
+        alone = _render_host_batch(ctx, [good], 0)[0]
         hosts = [f.alloc_host_targets() for f in (good, bad)]
         keep = []
         sc = [_host_scene(f, f.passes[0], h, keep) for f, h in zip((good, bad), hosts)]
         rc = ctx.render_host_batch((abi.Scene * 2)(*sc), 0)
         assert rc == abi.ERR_INDEX_OOB
-        assert (hosts[0]["color"] == 0).all() and (hosts[0]["depth"] == 1.0).all()
+        assert (hosts[1]["color"] == 0).all() and (hosts[1]["depth"] == 1.0).all()
+        for k in alone:
+            assert np.array_equal(alone[k].view(np.uint8), hosts[0][k].view(np.uint8)), k
+        assert (hosts[0]["color"] != 0).any()
+    finally:
+        ctx.close()
+
+
+@pytest.mark.parametrize("host_copy", [abi.HOST_COPY_STAGED, abi.HOST_COPY_DIRECT])
+def test_host_batch_sees_host_writes_between_calls(host_copy):
+    """The host clears the same target buffers between calls and edits the
+    vertices in place: every call renders what the host memory holds then."""
+    frames = [scenes.sphere_frame(seed=s, width=80, height=60, lon=16, lat=8) for s in range(3)]
+    ctx = _context(host_copy)
+    try:
+        hosts = [f.alloc_host_targets() for f in frames]
+        clean = [{k: v.copy() for k, v in h.items()} for h in hosts]
+        first = [{k: v.copy() for k, v in h.items()} for h in _render_host_batch(ctx, frames, 0, hosts=hosts)]
+        for _ in range(3):
+            for h, c in zip(hosts, clean):
+                for k in h:
+                    np.copyto(h[k], c[k])
+            _render_host_batch(ctx, frames, 0, hosts=hosts)
+            for a, b in zip(first, hosts):
+                for k in a:
+                    assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), k
+        # move every vertex of frame 0 off screen, in the host array the scene points at
+        v = frames[0].passes[0].vertices
+        saved = v.copy()
+        v.view(np.float32).reshape(frames[0].passes[0].nverts, -1)[:, 0] += 1e4
+        for h, c in zip(hosts, clean):
+            for k in h:
+                np.copyto(h[k], c[k])
+        _render_host_batch(ctx, frames, 0, hosts=hosts)
+        v[...] = saved
+        assert (hosts[0]["color"] == 0).all()
+        for a, b in zip(first[1:], hosts[1:]):
+            for k in a:
+                assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), k
     finally:
         ctx.close()
