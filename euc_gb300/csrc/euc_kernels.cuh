@@ -123,7 +123,8 @@ struct __align__(16) TriRec {
     uint32_t bx0, bx1, by0, by1;  // bbox clamped to the target (band clamp is per row)
     uint32_t v[3];                // vertex ids after the winding reversal
     uint32_t scene;
-    uint32_t flags;               // bit 0: all vertices pass the z clip
+    uint32_t flags;               // bit 0: all vertices pass the z clip; bit 1: every row spans the
+                                  // whole bbox; bit 2: every row lies in one band (k_setup)
     uint32_t pad[5];
 };
 static_assert(sizeof(TriRec) == 128, "TriRec must stay 128 bytes");
@@ -631,15 +632,13 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
                 // extent is below 128, so every row spans the whole bbox
                 // (triangles.rs:224-226) and k_raster skips the band and edge
                 // arithmetic
+                // bit 2: every row lies in one band (the band clamp is the
+                // bbox itself), so bit 1 alone decides the row kind
                 const bool one_band = by1 > by0 && by0 / s.gr == (by1 - 1) / s.gr;
                 const bool full_rows = one_band && (unsigned long long)(bx1 - bx0) * (by1 - by0) < 128ull;
-                r.flags = (noclip ? 1u : 0u) | (full_rows ? 2u : 0u);
+                r.flags = (noclip ? 1u : 0u) | (full_rows ? 2u : 0u) | (one_band ? 4u : 0u);
 #pragma unroll
                 for (int k = 0; k < 5; ++k) r.pad[k] = 0;
-                const float4 *src = reinterpret_cast<const float4 *>(&r);
-                float4 *dst = reinterpret_cast<float4 *>(recs + t);
-#pragma unroll
-                for (int k = 0; k < 8; ++k) dst[k] = src[k];
                 nrows = bx1 > bx0 ? by1 - by0 : 0u;
                 if (full_rows && (bx1 - bx0) * (by1 - by0) <= kTinyPixels) {
                     // a tiny primitive: walk its few pixels here exactly as
@@ -662,6 +661,12 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
                     if (!any) nrows = 0;
                 }
                 if (nrows) {
+                    // only a primitive with rows is ever read again (k_scan
+                    // keeps exactly those)
+                    const float4 *src = reinterpret_cast<const float4 *>(&r);
+                    float4 *dst = reinterpret_cast<float4 *>(recs + t);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) dst[k] = src[k];
                     cx0 = bx0;
                     cx1 = bx1;
                     cy0 = by0;
@@ -900,7 +905,7 @@ EUC_DEV void raster_line_step(const SceneDev &s, const TriRec &r, uint32_t t, ui
 EUC_DEV bool row_span(const SceneDev &s, const TriRec &r, uint32_t y, uint32_t &xs, uint32_t &xe) {
     const float yf = (float)y;
     bool full = r.flags & 2u;  // one band, extent < 128 (k_setup)
-    if (!full) {
+    if (!full && !(r.flags & 4u)) {  // rows in several bands
         // band of this row and the band-clamped bbox (pipeline.rs:341-360, triangles.rs:114-139)
         const uint32_t lo = (y / s.gr) * s.gr;
         const uint32_t hi = min(lo + s.gr, s.H);
@@ -1354,7 +1359,8 @@ EUC_DEV void resolve_direct_chunk(const SceneDev &s, const uint4 &cv, uint64_t l
         py[k] = i < area ? cv.y + ry : 0xFFFFFFFFu;
         key[k] = i < area ? vbuf[s.pix_base + (uint64_t)py[k] * s.W + px[k]] : 0ull;
     }
-#pragma unroll 1
+    // unrolled: the record and varyings gathers of the pixels overlap
+#pragma unroll
     for (int k = 0; k < kDirectPer; ++k) {
         uint32_t t;
         float z;
