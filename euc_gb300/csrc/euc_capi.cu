@@ -1213,7 +1213,8 @@ int host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int threads) {
         if (!pieces.empty()) {
             CUDA_TRY(cudaMemcpyAsync(d + tab, pieces.data(), pieces.size() * sizeof(CopyPiece), cudaMemcpyHostToDevice,
                                      nullptr));
-            k_copy_pieces<<<(unsigned)pieces.size(), kBlock, 0, nullptr>>>((const CopyPiece *)(d + tab));
+            k_copy_pieces<<<(unsigned)std::min<size_t>(pieces.size(), (size_t)ctx->nsm * 4), kBlock, 0, nullptr>>>(
+                (const CopyPiece *)(d + tab), (uint32_t)pieces.size());
             CUDA_TRY(cudaGetLastError());
             ctx->launches += 1;
         }

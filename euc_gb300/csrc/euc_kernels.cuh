@@ -1542,10 +1542,10 @@ __global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__
 }
 
 // ---------------------------------------------------------------------------
-// Host-buffer renders on a device that reads pageable host memory: one block
-// per piece of a region, 16-byte words with four loads in flight per thread
-// (the link's latency is microseconds), 4-byte or single-byte words where
-// the piece's ends are not aligned that far.
+// Host-buffer renders on a device that reads pageable host memory: blocks
+// take pieces of the regions in turn; 16-byte words with four loads in
+// flight per thread (the link's latency is microseconds), 4-byte or
+// single-byte words where a piece's ends are not aligned that far.
 // ---------------------------------------------------------------------------
 struct CopyPiece {
     const uint8_t *src;
@@ -1553,8 +1553,7 @@ struct CopyPiece {
     uint64_t bytes;
 };
 
-__global__ void __launch_bounds__(kBlock) k_copy_pieces(const CopyPiece *__restrict__ pieces) {
-    const CopyPiece p = pieces[blockIdx.x];
+EUC_DEV void copy_piece(const CopyPiece &p) {
     const uint64_t n = p.bytes;
     const uintptr_t al = (uintptr_t)p.src | (uintptr_t)p.dst | (uintptr_t)n;
     if ((al & 15) == 0) {
@@ -1577,6 +1576,10 @@ __global__ void __launch_bounds__(kBlock) k_copy_pieces(const CopyPiece *__restr
     } else {
         for (uint64_t i = threadIdx.x; i < n; i += kBlock) p.dst[i] = p.src[i];
     }
+}
+
+__global__ void __launch_bounds__(kBlock) k_copy_pieces(const CopyPiece *__restrict__ pieces, uint32_t npieces) {
+    for (uint32_t i = blockIdx.x; i < npieces; i += gridDim.x) copy_piece(pieces[i]);
 }
 
 // ---------------------------------------------------------------------------
