@@ -80,6 +80,8 @@ def parse():
     ap.add_argument("--no-graph", action="store_true", help="time plain euc_render_batch calls only")
     ap.add_argument("--rates", default="2000,10000,50000", help="serve: Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="serve: length of each rate's run")
+    ap.add_argument("--max-batch", type=int, default=256, help="serve: requests per batch at most")
+    ap.add_argument("--slots", type=int, default=3, help="serve: batches in flight at once")
     args = ap.parse_args()
     if args.workload != "batch":
         args.scenes = args.frames or WORKLOADS[args.workload][1]
@@ -532,7 +534,7 @@ def run_serve(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     frames = make_frames(args, rank)
-    srv = serve.Server(local, framebuffer_budget=40 << 30, max_batch=256, slots=3)
+    srv = serve.Server(local, framebuffer_budget=40 << 30, max_batch=args.max_batch, slots=args.slots)
     res = serve.Resident(srv)
     pins, keep, pool, outs = [], [], [], []
     for k, f in enumerate(frames):
@@ -580,7 +582,7 @@ def run_serve(args):
             "ms_per_step": 1e3 * args.serve_seconds, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators), meshes/textures resident",
             "config": {"workload": desc, "name": "serve", "pool": len(frames), "seed": args.seed,
-                       "rates": args.rates, "seconds_per_rate": args.serve_seconds, "max_batch": 256, "slots": 3,
+                       "rates": args.rates, "seconds_per_rate": args.serve_seconds, "max_batch": args.max_batch, "slots": args.slots,
                        "parallelism": "replicas" if world > 1 else "1 GPU"},
             "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
             "serving": runs,
