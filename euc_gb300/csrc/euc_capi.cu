@@ -1218,9 +1218,10 @@ int host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int threads) {
             CUDA_TRY(cudaGetLastError());
             ctx->launches += 1;
         }
-        if ((rc = run_batch(ctx, dev.data(), n, nullptr))) return rc;
+        // the kernels use the caller's buffers: none may still run when this returns
+        rc = run_batch(ctx, dev.data(), n, nullptr);
         CUDA_TRY(cudaStreamSynchronize(nullptr));
-        return first_scene_error(ctx);
+        return rc ? rc : first_scene_error(ctx);
     }
     if (ctx->h_pinned.cap < total) {
         if (ctx->h_pinned.p) CUDA_TRY(cudaFreeHost(ctx->h_pinned.p));
@@ -1243,7 +1244,10 @@ int host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int threads) {
     for (const Region &r : out) jobs.push_back({h + r.off, r.src, r.bytes});
     parallel_copy(jobs, threads);
     CUDA_TRY(cudaMemcpyAsync(d, h, off, cudaMemcpyHostToDevice, nullptr));
-    if ((rc = run_batch(ctx, dev.data(), n, nullptr))) return rc;
+    if ((rc = run_batch(ctx, dev.data(), n, nullptr))) {
+        CUDA_TRY(cudaStreamSynchronize(nullptr));  // the next call refills the staging
+        return rc;
+    }
     if (off > targets_at)
         CUDA_TRY(cudaMemcpyAsync(h + targets_at, d + targets_at, off - targets_at, cudaMemcpyDeviceToHost, nullptr));
     CUDA_TRY(cudaStreamSynchronize(nullptr));
