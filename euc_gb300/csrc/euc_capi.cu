@@ -543,13 +543,14 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
     if ((rc = grow(ctx->cov, ns * sizeof(uint4)))) return rc;
     if ((rc = grow(ctx->plan, 2 * (ns + 1) * sizeof(uint64_t)))) return rc;
     if (gin && (rc = grow(ctx->galive, tri))) return rc;
-    // staging: scene table | vtx bases | tri bases | resolve bases | geometry bases | uniforms
+    // staging: scene table | vtx bases | resolve bases | geometry bases |
+    // scene of each setup chunk | uniforms
     const size_t off_sc = 0;
     const size_t off_vb = pad_up(ns * sizeof(SceneDev), 16);
-    const size_t off_tb = off_vb + pad_up(ns * sizeof(uint64_t), 16);
-    const size_t off_rb = off_tb + pad_up(ns * sizeof(uint64_t), 16);
+    const size_t off_rb = off_vb + pad_up(ns * sizeof(uint64_t), 16);
     const size_t off_gb = off_rb + pad_up(ns * sizeof(uint64_t), 16);
-    size_t off_u = off_gb + pad_up(ns * sizeof(uint64_t), 16);
+    const size_t off_cs = off_gb + pad_up(ns * sizeof(uint64_t), 16);
+    size_t off_u = off_cs + pad_up(nchunks * sizeof(uint32_t), 16);
     std::vector<size_t> uoff(ns);
     for (int i = 0; i < ns; ++i) {
         uoff[i] = off_u;
@@ -568,24 +569,28 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
     uint8_t *h = (uint8_t *)(so ? so->host : slot->host);
     uint8_t *dv = (uint8_t *)(so ? so->dev : slot->dev);
     SceneDev *hsc = (SceneDev *)(h + off_sc);
-    uint64_t *hvb = (uint64_t *)(h + off_vb), *htb = (uint64_t *)(h + off_tb), *hrb = (uint64_t *)(h + off_rb),
-             *hgb = (uint64_t *)(h + off_gb);
+    uint64_t *hvb = (uint64_t *)(h + off_vb), *hrb = (uint64_t *)(h + off_rb), *hgb = (uint64_t *)(h + off_gb);
+    uint32_t *hcs = (uint32_t *)(h + off_cs);
+    for (int i = 0; i < ns; ++i) {  // scene ranges of primitives are padded to whole setup chunks
+        const uint64_t c0 = plans[i].d.tri_base / kBlock, c1 = (i + 1 < ns ? plans[i + 1].d.tri_base : tri) / kBlock;
+        for (uint64_t c = c0; c < c1; ++c) hcs[c] = (uint32_t)i;
+    }
     for (int i = 0; i < ns; ++i) {
         std::memcpy(h + uoff[i], plans[i].uniforms, plans[i].usize);
         plans[i].d.uniforms = dv + uoff[i];
         hsc[i] = plans[i].d;
         hvb[i] = plans[i].d.vtx_base;
-        htb[i] = plans[i].d.tri_base;
         hrb[i] = res_base[i];
         hgb[i] = gin_base[i];
     }
     CUDA_TRY(cudaMemcpyAsync(dv, h, off_u, cudaMemcpyHostToDevice, st));
     const SceneDev *dsc = (const SceneDev *)(dv + off_sc);
-    const uint64_t *dvb = (const uint64_t *)(dv + off_vb), *dtb = (const uint64_t *)(dv + off_tb),
-                   *drb = (const uint64_t *)(dv + off_rb), *dgb = (const uint64_t *)(dv + off_gb);
+    const uint64_t *dvb = (const uint64_t *)(dv + off_vb), *drb = (const uint64_t *)(dv + off_rb),
+                   *dgb = (const uint64_t *)(dv + off_gb);
     CUDA_TRY(cudaMemsetAsync(ctx->err.p, 0, ns * sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(ctx->stats.p, 0, ns * sizeof(SceneStats), st));
     CUDA_TRY(cudaMemsetAsync(ctx->cov.p, 0xFF, ns * sizeof(uint4), st));  // empty rectangles
+    CUDA_TRY(cudaMemsetAsync(ctx->chunk_sums.p, 0, nchunks * sizeof(uint2), st));
     // vertex stage, one launch per shader kind
     cudaEvent_t e0 = prof_event(ctx, st);
     for (int a = 0; a < ns;) {
@@ -609,8 +614,9 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
         a = b;
     }
     cudaEvent_t e1 = prof_event(ctx, st);
-    k_setup<<<(unsigned)nchunks, kBlock, 0, st>>>(dsc, dtb, ns, (const float4 *)ctx->clip.p, (TriRec *)ctx->recs.p,
-                                                   (uint32_t *)ctx->rows.p, (uint2 *)ctx->chunk_sums.p, (int *)ctx->err.p,
+    k_setup<<<(unsigned)nchunks, kBlock, 0, st>>>(dsc, (const uint32_t *)(dv + off_cs), (const float4 *)ctx->clip.p,
+                                                   (TriRec *)ctx->recs.p, (uint32_t *)ctx->rows.p,
+                                                   (uint2 *)ctx->chunk_sums.p, (int *)ctx->err.p,
                                                    (SceneStats *)ctx->stats.p, (uint4 *)ctx->cov.p,
                                                    (const uint8_t *)ctx->galive.p);
     cudaEvent_t e2 = prof_event(ctx, st);
@@ -1469,9 +1475,10 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
     CUDA_TRY(cudaMemsetAsync(a + kNaOffErr, 0, sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(a + kNaOffStats, 0, sizeof(SceneStats), st));
     CUDA_TRY(cudaMemsetAsync(a + kNaOffCov, 0xFF, sizeof(uint4), st));
+    CUDA_TRY(cudaMemsetAsync(a + kNaOffChunks, 0, (tri / kBlock) * sizeof(uint2), st));
     t_na_nsm = nsm;
     na_dispatch(true, d.shader, dsc, zero_base, vtx / kBlock, a, st);
-    k_setup<<<(unsigned)(tri / kBlock), kBlock, 0, st>>>(dsc, zero_base, 1, (const float4 *)(a + kNaOffClip),
+    k_setup<<<(unsigned)(tri / kBlock), kBlock, 0, st>>>(dsc, nullptr, (const float4 *)(a + kNaOffClip),
                                                           (TriRec *)(a + kNaOffRecs), (uint32_t *)(a + kNaOffRows),
                                                           (uint2 *)(a + kNaOffChunks), (int *)(a + kNaOffErr),
                                                           (SceneStats *)(a + kNaOffStats), (uint4 *)(a + kNaOffCov),

@@ -480,18 +480,17 @@ constexpr uint32_t kTinyPixels = 4;
 // ---------------------------------------------------------------------------
 // k_setup: triangles.rs:55-199, once per primitive (euc repeats it per band;
 // only the bbox clamp depends on the band and that is applied per row).
+// Block b sets up primitives [b * kBlock, (b + 1) * kBlock), all of scene
+// chunk_scene[b] (null: scene 0); chunk_sums must be zero at launch.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ tri_base,
-                                                  int nsc, const float4 *__restrict__ clip, TriRec *__restrict__ recs,
+__global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ sc,
+                                                  const uint32_t *__restrict__ chunk_scene,
+                                                  const float4 *__restrict__ clip, TriRec *__restrict__ recs,
                                                   uint32_t *__restrict__ rows, uint2 *__restrict__ chunk_sums,
                                                   int *__restrict__ err, SceneStats *__restrict__ stats,
                                                   uint4 *__restrict__ cov, const uint8_t *__restrict__ galive) {
-    __shared__ int s_scene;
-    __shared__ uint32_t s_red[2][kBlock / 32];
     const uint64_t t = (uint64_t)blockIdx.x * kBlock + threadIdx.x;
-    if (threadIdx.x == 0) s_scene = find_scene(tri_base, nsc, (uint64_t)blockIdx.x * kBlock);
-    __syncthreads();
-    const int si = s_scene;
+    const int si = chunk_scene ? (int)chunk_scene[blockIdx.x] : 0;
     const SceneDev &s = sc[si];
     const uint64_t lt = t - s.tri_base;
     uint32_t nrows = 0, culled = 0;
@@ -601,11 +600,15 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
                     dyw[i] = (wy - o[i]) * (1.0f / 1000.0f);
                 }
                 // vertices by height (triangles.rs:148-171)
-                const int ord_tab[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
-                int oi;
-                if (scr[0][1] == mny) oi = scr[1][1] < scr[2][1] ? 0 : 1;
-                else if (scr[1][1] == mny) oi = scr[0][1] < scr[2][1] ? 2 : 3;
-                else oi = scr[0][1] < scr[1][1] ? 4 : 5;
+                // (selects, not an index table: the vertices stay in registers)
+                int oy[3];
+                if (scr[0][1] == mny) {
+                    oy[0] = 0; oy[1] = scr[1][1] < scr[2][1] ? 1 : 2; oy[2] = 3 - oy[1];
+                } else if (scr[1][1] == mny) {
+                    oy[0] = 1; oy[1] = scr[0][1] < scr[2][1] ? 0 : 2; oy[2] = 2 - oy[1];
+                } else {
+                    oy[0] = 2; oy[1] = scr[0][1] < scr[1][1] ? 0 : 1; oy[2] = 1 - oy[1];
+                }
                 // z-clip class (triangles.rs:173)
                 bool noclip = true;
                 if (s.zclip) {
@@ -622,8 +625,8 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
                 }
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    r.vby[2 * k] = scr[ord_tab[oi][k]][0];
-                    r.vby[2 * k + 1] = scr[ord_tab[oi][k]][1];
+                    r.vby[2 * k] = oy[k] == 0 ? scr[0][0] : oy[k] == 1 ? scr[1][0] : scr[2][0];
+                    r.vby[2 * k + 1] = oy[k] == 0 ? scr[0][1] : oy[k] == 1 ? scr[1][1] : scr[2][1];
                 }
                 r.bx0 = bx0; r.bx1 = bx1; r.by0 = by0; r.by1 = by1;
                 r.v[0] = vid[0]; r.v[1] = vid[1]; r.v[2] = vid[2];
@@ -687,17 +690,14 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
             atomicMin(&cov[si].w, m3);
         }
     }
-    // per-block sums for the scan, and the culled count of this scene
+    // per-block sums for the scan (zeroed before the launch; each warp adds
+    // its own, no block barrier), and the culled count of this scene
     const uint32_t live = nrows ? 1u : 0u;
     uint32_t wl = warp_sum(live), wr = warp_sum(nrows), wc = warp_sum(culled);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) { s_red[0][warp] = wl; s_red[1][warp] = wr; }
-    if (lane == 0 && wc) atomicAdd(&stats[si].culled, (unsigned long long)wc);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t a = 0, b = 0;
-        for (int w = 0; w < kBlock / 32; ++w) { a += s_red[0][w]; b += s_red[1][w]; }
-        chunk_sums[blockIdx.x] = make_uint2(a, b);
+    if ((threadIdx.x & 31) == 0) {
+        if (wl) atomicAdd(&chunk_sums[blockIdx.x].x, wl);
+        if (wr) atomicAdd(&chunk_sums[blockIdx.x].y, wr);
+        if (wc) atomicAdd(&stats[si].culled, (unsigned long long)wc);
     }
 }
 

@@ -908,6 +908,10 @@ int oracle_render(const euc_pipeline_desc *d, const void *uniforms, size_t usize
                   const void *verts, size_t nverts, const uint32_t *idx, size_t nidx, const euc_target *pixel,
                   const euc_target *depth, int threads, oracle_stats *st) {
     if (!d || !lay || !uniforms) return EUC_ERR_INVALID;
+    // the C ABI's enum ranges (euc's Rust enums cannot hold other values)
+    if (d->depth_test > EUC_TEST_GREATER || d->cull > EUC_CULL_FRONT || d->y_axis > EUC_Y_UP ||
+        d->blend > EUC_BLEND_ALPHA)
+        return EUC_ERR_INVALID;
     if (d->primitives > EUC_PRIM_LINE_LIST || d->geometry > EUC_GEOM_DISCARD) return EUC_ERR_INVALID;
     if (d->geometry != EUC_GEOM_NONE && d->primitives != EUC_PRIM_TRIANGLE_LIST) return EUC_ERR_INVALID;
     if (nverts && !verts) return EUC_ERR_INVALID;
