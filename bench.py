@@ -461,6 +461,9 @@ def run_gpu(args):
         "staged through page-locked memory by host threads, one copy each way"
 
     alg_bytes = sum(f.algorithmic_bytes() for f in specs)
+    # each step also clears every target first, as euc's own bench loop does
+    # (benches/teapot.rs:182-184): one more write of each target
+    clear_bytes = sum(t.width * t.height * t.bpp for f in specs for t in f.targets)
     dom = max(stage_ms, key=lambda k: stage_ms[k])
     dom_ms = stage_ms[dom] / args.steps
     peak, peak_kind = load_peaks()
@@ -499,7 +502,9 @@ def run_gpu(args):
                          "traffic": traffic.get(args.workload, {}).get("k_" + dom) if traffic else None},
             # the whole step (every stage, launch gaps included) against the same peak
             "pipeline_roofline": {"achieved": alg_bytes / (ms_step / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
-                                  "frac": alg_bytes / (ms_step / 1e3) / 1e9 / peak, "peak_kind": peak_kind},
+                                  "frac": alg_bytes / (ms_step / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
+                                  "clear_bytes_per_step": clear_bytes,
+                                  "frac_with_clear": (alg_bytes + clear_bytes) / (ms_step / 1e3) / 1e9 / peak},
             "e2e": {"value": e2e, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "path": "euc_render_host_batch (host buffers, blocking; one call per pass)",
                     "host_copy": host_copy,
