@@ -228,15 +228,20 @@ def host_bytes(frames):
 
 
 def run_e2e(ctx, frames, reps):
-    """Blocking host-buffer renders (euc_render_host), one per scene pass."""
+    """Blocking host-buffer renders (euc_render_host), one per scene pass.  The
+    host targets are reset to their clear values before each repetition,
+    outside the timed region."""
     from euc_gb300 import abi
     hosts = [f.alloc_host_targets() for f in frames]
     clean = [{k: v.copy() for k, v in h.items()} for h in hosts]
 
-    def one_pass():
-        for f, h, c in zip(frames, hosts, clean):
+    def reset():
+        for h, c in zip(hosts, clean):
             for k in h:
                 np.copyto(h[k], c[k])
+
+    def one_pass():
+        for f, h in zip(frames, hosts):
             for p in f.passes:
                 uni, keep = p.bind_uniforms(lambda src: f.host_texture_ptr(src, h))
                 pix = h[p.pixel] if p.pixel else None
@@ -252,11 +257,15 @@ def run_e2e(ctx, frames, reps):
                 if rc != abi.OK:
                     raise RuntimeError("euc_render_host failed: %d" % rc)
                 del keep
+    reset()
     one_pass()  # warm-up (allocations)
-    t0 = time.perf_counter()
+    total = 0.0
     for _ in range(reps):
+        reset()
+        t0 = time.perf_counter()
         one_pass()
-    return reps * len(frames) / (time.perf_counter() - t0)
+        total += time.perf_counter() - t0
+    return reps * len(frames) / total
 
 
 def run_e2e_batch(ctx, frames, reps):
