@@ -452,6 +452,10 @@ def run_gpu(args):
             fr.render_frame(ctx, df, stream, clear=False)
     per_scene = e2e = e2e_per_scene = None
     if not args.only_batched:
+        # the per-scene paths run with the default launch shape (the tuned one
+        # is chosen for the batch)
+        tuned = ctx.get_tuning()
+        ctx.set_tuning(None)
         per_scene_pass()
         torch.cuda.synchronize()
         reps = max(2, args.steps // 4)
@@ -462,8 +466,9 @@ def run_gpu(args):
         p1.record(stream)
         torch.cuda.synchronize()
         per_scene = args.scenes / (p0.elapsed_time(p1) / reps / 1e3)
-        e2e = run_e2e_batch(ctx, specs, reps=max(2, min(args.steps, 5)))
         e2e_per_scene = run_e2e(ctx, specs, reps=1)
+        ctx.set_tuning(tuned)
+        e2e = run_e2e_batch(ctx, specs, reps=max(2, min(args.steps, 5)))
     h2d, d2h = host_bytes(specs)
     host_copy = ("in place: kernels read vertices and indices and update targets in host memory over "
                  "NVLink-C2C; one kernel gathers the textures") if ctx.host_copy_direct() else \

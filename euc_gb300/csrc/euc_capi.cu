@@ -48,7 +48,7 @@ struct euc_ctx {
     int nsm = 0;
     DevBuf clip, vdata, recs, rows, chunk_sums, live_tri, live_rowoff, totals, vbuf, err, stats, cov;
     DevBuf obsum, frags;  // ordered path: pixel-scan block sums, fragment lists
-    DevBuf plan;          // k_plan: k_init and k_resolve chunk bases (2 x (scenes + 1))
+    DevBuf plan;          // plan_chunks: k_init and k_resolve chunk bases (2 x (scenes + 1))
     DevBuf galive;        // geometry stage: 1 per output slot that holds a triangle
     int raster_blocks = 0;  // resident k_raster blocks per SM
     bool pageable = false;  // kernels may access pageable host memory (cudaDevAttrPageableMemoryAccess)
@@ -386,7 +386,7 @@ void launch_vertex(const SceneDev *sc, const uint64_t *vb, int s0, int s1, uint6
     if (nblk) k_vertex<F><<<(unsigned)nblk, kBlock, 0, st>>>(sc, vb, s0, s1, blk0, (float4 *)ctx->clip.p, (float *)ctx->vdata.p);
 }
 
-// rbase: the device chunk bases of k_plan; nblk: an upper bound of the
+// rbase: the device chunk bases of plan_chunks; nblk: an upper bound of the
 // chunks of scenes [s0, s1) (their whole targets), which sizes the grid.
 template <class F>
 void launch_geometry(const SceneDev *sc, const uint64_t *gb, int s0, int s1, uint64_t blk0, uint64_t nblk, euc_ctx *ctx,
@@ -587,10 +587,8 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
     const SceneDev *dsc = (const SceneDev *)(dv + off_sc);
     const uint64_t *dvb = (const uint64_t *)(dv + off_vb), *drb = (const uint64_t *)(dv + off_rb),
                    *dgb = (const uint64_t *)(dv + off_gb);
-    CUDA_TRY(cudaMemsetAsync(ctx->err.p, 0, ns * sizeof(int), st));
-    CUDA_TRY(cudaMemsetAsync(ctx->stats.p, 0, ns * sizeof(SceneStats), st));
-    CUDA_TRY(cudaMemsetAsync(ctx->cov.p, 0xFF, ns * sizeof(uint4), st));  // empty rectangles
-    CUDA_TRY(cudaMemsetAsync(ctx->chunk_sums.p, 0, nchunks * sizeof(uint2), st));
+    k_prep<<<(unsigned)((std::max<uint64_t>((uint64_t)ns, nchunks) + kBlock - 1) / kBlock), kBlock, 0, st>>>(
+        (int *)ctx->err.p, (SceneStats *)ctx->stats.p, (uint4 *)ctx->cov.p, ns, (uint2 *)ctx->chunk_sums.p, nchunks);
     // vertex stage, one launch per shader kind
     cudaEvent_t e0 = prof_event(ctx, st);
     for (int a = 0; a < ns;) {
@@ -620,21 +618,30 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
                                                    (SceneStats *)ctx->stats.p, (uint4 *)ctx->cov.p,
                                                    (const uint8_t *)ctx->galive.p);
     cudaEvent_t e2 = prof_event(ctx, st);
-    k_scan<<<(unsigned)nscan, kBlock, 0, st>>>((const uint32_t *)ctx->rows.p, (const uint2 *)ctx->chunk_sums.p, tri,
-                                               (uint32_t *)ctx->live_tri.p, (uint64_t *)ctx->live_rowoff.p,
-                                               (unsigned long long *)ctx->totals.p);
     uint64_t *const ibase = (uint64_t *)ctx->plan.p, *const rbase = ibase + ns + 1;
-    k_plan<<<1, kBlock, 0, st>>>(dsc, ns, (const uint4 *)ctx->cov.p, ibase, rbase);
+    k_scan_plan<<<(unsigned)nscan + 1, kBlock, 0, st>>>((const uint32_t *)ctx->rows.p, (const uint2 *)ctx->chunk_sums.p,
+                                                        tri, (uint32_t *)ctx->live_tri.p, (uint64_t *)ctx->live_rowoff.p,
+                                                        (unsigned long long *)ctx->totals.p, (uint32_t)nscan, dsc, ns,
+                                                        (const uint4 *)ctx->cov.p, ibase, rbase);
     cudaEvent_t e3 = prof_event(ctx, st);
     const euc_tuning &tu = ctx->tune;
-    const uint64_t ichunks = (pix + kInitChunk - 1) / kInitChunk + ns;  // bounds the chunks k_plan counts
+    const uint64_t ichunks = (pix + kInitChunk - 1) / kInitChunk + ns;  // bounds the chunks plan_chunks counts
     k_init<<<chunk_grid(ichunks, ctx->nsm, tu.chunk_group, tu.chunk_blocks_per_sm), kBlock, 0, st>>>(
         dsc, ibase, ns, (const uint4 *)ctx->cov.p, (unsigned long long *)ctx->vbuf.p,
         chunk_group(ichunks, ctx->nsm, tu.chunk_group, tu.chunk_blocks_per_sm));
     cudaEvent_t e4 = prof_event(ctx, st);
-    const unsigned rgrid = (unsigned)(ctx->nsm * (tu.raster_blocks_per_sm ? (int)tu.raster_blocks_per_sm
-                                                                           : ctx->raster_blocks));
     const int witems = tu.raster_warp_rows ? (int)tu.raster_warp_rows : kWarpItems;
+    // persistent blocks, but no more than the items can keep busy: a
+    // primitive slot has at most max(W, H) + 2 items (rows, or line steps)
+    uint64_t item_bound = 0;
+    for (int i = 0; i < ns; ++i) {
+        const uint64_t slots = (i + 1 < ns ? plans[i + 1].d.tri_base : tri) - plans[i].d.tri_base;
+        item_bound += slots * ((uint64_t)std::max(plans[i].d.W, plans[i].d.H) + 2);
+    }
+    const uint64_t busy = (item_bound + (uint64_t)witems * (kBlock / 32) - 1) / ((uint64_t)witems * (kBlock / 32));
+    const unsigned rgrid = (unsigned)std::max<uint64_t>(
+        1, std::min<uint64_t>(busy, (uint64_t)ctx->nsm * (tu.raster_blocks_per_sm ? tu.raster_blocks_per_sm
+                                                                                   : (uint32_t)ctx->raster_blocks)));
     const bool probe = tu.raster_probe == 1;
     k_raster<<<rgrid, kBlock, 0, st>>>(dsc, (const TriRec *)ctx->recs.p, (const uint32_t *)ctx->live_tri.p,
                                        (const uint64_t *)ctx->live_rowoff.p, (unsigned long long *)ctx->totals.p,
@@ -1335,7 +1342,7 @@ constexpr size_t kNaOffErr = kNaStage;
 constexpr size_t kNaOffStats = kNaOffErr + 256;
 constexpr size_t kNaOffTotals = kNaOffStats + 256;
 constexpr size_t kNaOffCov = kNaOffTotals + 64;   // inside the 256-byte totals region
-constexpr size_t kNaOffPlan = kNaOffTotals + 128;  // k_plan's 2 x 2 chunk bases, same region
+constexpr size_t kNaOffPlan = kNaOffTotals + 128;  // plan_chunks's 2 x 2 chunk bases, same region
 constexpr size_t kNaOffClip = kNaOffTotals + 256;
 constexpr size_t kNaOffVdata = kNaOffClip + kNaMaxVerts * sizeof(float4);
 constexpr size_t kNaOffRecs = kNaOffVdata + kNaMaxVerts * kNaMaxNV * sizeof(float);
@@ -1472,10 +1479,9 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
     CUDA_TRY(cudaMemcpyAsync(a, stage, off_u + p.usize, cudaMemcpyHostToDevice, st));
     const SceneDev *dsc = (const SceneDev *)a;
     const uint64_t *zero_base = (const uint64_t *)(a + off_b);  // every base is 0 for a single scene
-    CUDA_TRY(cudaMemsetAsync(a + kNaOffErr, 0, sizeof(int), st));
-    CUDA_TRY(cudaMemsetAsync(a + kNaOffStats, 0, sizeof(SceneStats), st));
-    CUDA_TRY(cudaMemsetAsync(a + kNaOffCov, 0xFF, sizeof(uint4), st));
-    CUDA_TRY(cudaMemsetAsync(a + kNaOffChunks, 0, (tri / kBlock) * sizeof(uint2), st));
+    k_prep<<<(unsigned)((tri / kBlock + kBlock - 1) / kBlock), kBlock, 0, st>>>(
+        (int *)(a + kNaOffErr), (SceneStats *)(a + kNaOffStats), (uint4 *)(a + kNaOffCov), 1,
+        (uint2 *)(a + kNaOffChunks), tri / kBlock);
     t_na_nsm = nsm;
     na_dispatch(true, d.shader, dsc, zero_base, vtx / kBlock, a, st);
     k_setup<<<(unsigned)(tri / kBlock), kBlock, 0, st>>>(dsc, nullptr, (const float4 *)(a + kNaOffClip),
@@ -1483,11 +1489,12 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
                                                           (uint2 *)(a + kNaOffChunks), (int *)(a + kNaOffErr),
                                                           (SceneStats *)(a + kNaOffStats), (uint4 *)(a + kNaOffCov),
                                                           nullptr);
-    k_scan<<<(unsigned)((tri + kScanBlock - 1) / kScanBlock), kBlock, 0, st>>>(
-        (const uint32_t *)(a + kNaOffRows), (const uint2 *)(a + kNaOffChunks), tri, (uint32_t *)(a + kNaOffLiveTri),
-        (uint64_t *)(a + kNaOffLiveOff), (unsigned long long *)(a + kNaOffTotals));
     uint64_t *const ibase = (uint64_t *)(a + kNaOffPlan), *const rbase = ibase + 2;
-    k_plan<<<1, kBlock, 0, st>>>(dsc, 1, (const uint4 *)(a + kNaOffCov), ibase, rbase);
+    const uint32_t nscan = (uint32_t)((tri + kScanBlock - 1) / kScanBlock);
+    k_scan_plan<<<nscan + 1, kBlock, 0, st>>>((const uint32_t *)(a + kNaOffRows), (const uint2 *)(a + kNaOffChunks),
+                                              tri, (uint32_t *)(a + kNaOffLiveTri), (uint64_t *)(a + kNaOffLiveOff),
+                                              (unsigned long long *)(a + kNaOffTotals), nscan, dsc, 1,
+                                              (const uint4 *)(a + kNaOffCov), ibase, rbase);
     const uint64_t ichunks = (pix + kInitChunk - 1) / kInitChunk + 1;
     k_init<<<chunk_grid(ichunks, nsm), kBlock, 0, st>>>(dsc, ibase, 1, (const uint4 *)(a + kNaOffCov),
                                                          (unsigned long long *)(a + kNaOffVbuf),

@@ -8,8 +8,11 @@
 //                 (index.rs:52-54), flip, perspective divide, winding, cull /
 //                 reverse, weight matrix, screen bbox, per-pixel weight deltas,
 //                 vertices by y, z-clip class (triangles.rs:55-199)
-//   k_scan        exclusive scan of per-primitive row counts, compaction of the
-//                 primitives that cover at least one row
+//   k_prep        per batch: clears the error, statistics, covered-rectangle
+//                 and setup-sum entries
+//   k_scan_plan   exclusive scan of per-primitive row counts, compaction of the
+//                 primitives that cover at least one row; one more block
+//                 plans the init / resolve chunks of every scene
 //   k_init        per pixel: the visibility key of the depth already in place
 //   k_raster      one thread per (primitive, row): euc's serial f32 weight
 //                 walk along the row span (triangles.rs:219-303), inside test,
@@ -35,7 +38,7 @@
 namespace eucg {
 
 constexpr int kBlock = 256;           // threads per block in every kernel
-constexpr int kScanPer = 8;           // primitives per thread in k_scan
+constexpr int kScanPer = 8;           // primitives per thread in the scan
 constexpr int kScanBlock = kBlock * kScanPer;
 
 // VertexData floats per vertex in vdata[]: more than four are padded to a
@@ -664,7 +667,7 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
                     if (!any) nrows = 0;
                 }
                 if (nrows) {
-                    // only a primitive with rows is ever read again (k_scan
+                    // only a primitive with rows is ever read again (the scan
                     // keeps exactly those)
                     const float4 *src = reinterpret_cast<const float4 *>(&r);
                     float4 *dst = reinterpret_cast<float4 *>(recs + t);
@@ -702,17 +705,16 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
 }
 
 // ---------------------------------------------------------------------------
-// k_scan: stable compaction of the primitives that cover at least one row
-// (submission order kept) and the exclusive scan of their row counts.  Block
-// b covers primitives [b*kScanBlock, (b+1)*kScanBlock), i.e. the setup
-// chunks [b*kScanPer, (b+1)*kScanPer).  totals[0] = live primitives,
-// totals[1] = rows, totals[2] = k_raster's work counter (reset here, so that
-// no separate memset is needed).
+// scan_block (in k_scan_plan): stable compaction of the primitives that
+// cover at least one row (submission order kept) and the exclusive scan of
+// their row counts.  Block b covers primitives [b*kScanBlock,
+// (b+1)*kScanBlock), i.e. the setup chunks [b*kScanPer, (b+1)*kScanPer).
+// totals[0] = live primitives, totals[1] = rows, totals[2] = k_raster's work
+// counter (reset here, so that no separate memset is needed).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_scan(const uint32_t *__restrict__ rows, const uint2 *__restrict__ chunk_sums,
-                                                 uint64_t ntri, uint32_t *__restrict__ live_tri,
-                                                 uint64_t *__restrict__ live_rowoff,
-                                                 unsigned long long *__restrict__ totals) {
+EUC_DEV void scan_block(const uint32_t *__restrict__ rows, const uint2 *__restrict__ chunk_sums, uint64_t ntri,
+                        uint32_t *__restrict__ live_tri, uint64_t *__restrict__ live_rowoff,
+                        unsigned long long *__restrict__ totals, uint32_t nscan) {
     __shared__ unsigned long long s_a[kBlock / 32 + 1];
     __shared__ unsigned long long s_pre[2];
     // prefix of all earlier chunks
@@ -751,7 +753,7 @@ __global__ void __launch_bounds__(kBlock) k_scan(const uint32_t *__restrict__ ro
             orr += r[k];
         }
     }
-    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == kBlock - 1) {
+    if (blockIdx.x == nscan - 1 && threadIdx.x == kBlock - 1) {
         totals[0] = base_l + bl;
         totals[1] = base_r + br;
         totals[2] = 0;  // work counter of k_raster, phase 0
@@ -777,7 +779,7 @@ __host__ __device__ inline uint64_t rect_area(const uint4 &c) {
 // grid-strided, so the scene table is searched once per group rather than
 // once per chunk (the host picks group = 1 for small launches, up to
 // kChunkGroup for large batches).  The chunks of every scene are counted on
-// the device by k_plan, from the covered rectangle k_setup found, so no block
+// the device by plan_chunks, from the covered rectangle k_setup found, so no block
 // is spent on pixels that no primitive reaches.
 constexpr int kChunkGroup = 16;
 
@@ -794,7 +796,7 @@ EUC_DEV int advance_scene(const uint64_t *base, int nsc, int si, uint64_t c) {
     return si;
 }
 
-// ibase: the first k_init chunk of every scene (nsc + 1 entries, k_plan).
+// ibase: the first k_init chunk of every scene (nsc + 1 entries, plan_chunks).
 __global__ void __launch_bounds__(kBlock) k_init(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ ibase,
                                                  int nsc, const uint4 *__restrict__ cov,
                                                  unsigned long long *__restrict__ vbuf, uint32_t group) {
@@ -1297,9 +1299,8 @@ __host__ __device__ inline uint64_t resolve_blocks(const SceneDev &s) {
 
 // Chunk bases of k_init and k_resolve per scene, from the covered rectangles
 // (exclusive prefix sums, nsc + 1 entries each).  One block, any nsc.
-__global__ void __launch_bounds__(kBlock) k_plan(const SceneDev *__restrict__ sc, int nsc,
-                                                 const uint4 *__restrict__ cov, uint64_t *__restrict__ ibase,
-                                                 uint64_t *__restrict__ rbase) {
+EUC_DEV void plan_chunks(const SceneDev *__restrict__ sc, int nsc, const uint4 *__restrict__ cov,
+                         uint64_t *__restrict__ ibase, uint64_t *__restrict__ rbase) {
     __shared__ uint64_t s_a[kBlock / 32 + 1];
     uint64_t ci = 0, cr = 0;
     for (int s0 = 0; s0 < nsc; s0 += kBlock) {
@@ -1330,6 +1331,35 @@ __global__ void __launch_bounds__(kBlock) k_plan(const SceneDev *__restrict__ sc
         ibase[nsc] = ci;
         rbase[nsc] = cr;
     }
+}
+
+// The scan of the setup's row counts (blocks 0 .. nscan - 1, scan_block) and
+// the chunk plan of init / resolve (block nscan, plan_chunks): independent
+// work after k_setup, in one launch.
+__global__ void __launch_bounds__(kBlock) k_scan_plan(const uint32_t *__restrict__ rows,
+                                                      const uint2 *__restrict__ chunk_sums, uint64_t ntri,
+                                                      uint32_t *__restrict__ live_tri,
+                                                      uint64_t *__restrict__ live_rowoff,
+                                                      unsigned long long *__restrict__ totals, uint32_t nscan,
+                                                      const SceneDev *__restrict__ sc, int nsc,
+                                                      const uint4 *__restrict__ cov, uint64_t *__restrict__ ibase,
+                                                      uint64_t *__restrict__ rbase) {
+    if (blockIdx.x == nscan) plan_chunks(sc, nsc, cov, ibase, rbase);
+    else scan_block(rows, chunk_sums, ntri, live_tri, live_rowoff, totals, nscan);
+}
+
+// Per batch, before k_setup: no errors, zero statistics, empty covered
+// rectangles, zero setup-chunk sums.
+__global__ void __launch_bounds__(kBlock) k_prep(int *__restrict__ err, SceneStats *__restrict__ stats,
+                                                 uint4 *__restrict__ cov, int nsc, uint2 *__restrict__ chunk_sums,
+                                                 uint64_t nchunks) {
+    const uint64_t i = (uint64_t)blockIdx.x * kBlock + threadIdx.x;
+    if (i < (uint64_t)nsc) {
+        err[i] = 0;
+        stats[i] = SceneStats{};
+        cov[i] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+    }
+    if (i < nchunks) chunk_sums[i] = make_uint2(0u, 0u);
 }
 
 template <class F>
@@ -1509,7 +1539,7 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
 }
 
 // Blocks walk groups of `group` chunks (grid-strided) of the scenes
-// [s_begin, s_end); rbase (global scene index, from k_plan) holds the first
+// [s_begin, s_end); rbase (global scene index, from plan_chunks) holds the first
 // chunk of each.
 template <class F>
 __global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ rbase,
