@@ -33,6 +33,7 @@
 // result is bit-identical to euc's loop while rows run in parallel.
 #pragma once
 
+#include <cstddef>
 #include "euc_device.cuh"
 
 namespace eucg {
@@ -117,20 +118,51 @@ struct SceneDev {
 };
 
 // Per-primitive record written by k_setup (128 bytes, 16-byte aligned).
+// The fields are ordered so that a triangle's raster walk needs the first six
+// 16-byte words and its shading words 0-2 and 6 (load_rec).
 struct __align__(16) TriRec {
     float o[3];    // w_hom_origin   (triangles.rs:143)
     float dx[3];   // w_hom_dx       (triangles.rs:144)
     float dy[3];   // w_hom_dy       (triangles.rs:145)
     float zc[3];   // clip-space z of the (reordered) vertices (triangles.rs:269)
-    float vby[6];  // screen vertices ordered by y (triangles.rs:148-171)
     uint32_t bx0, bx1, by0, by1;  // bbox clamped to the target (band clamp is per row)
-    uint32_t v[3];                // vertex ids after the winding reversal
+    float vby[6];  // screen vertices ordered by y (triangles.rs:148-171)
     uint32_t scene;
     uint32_t flags;               // bit 0: all vertices pass the z clip; bit 1: every row spans the
                                   // whole bbox; bit 2: every row lies in one band (k_setup)
+    uint32_t v[3];                // vertex ids after the winding reversal
     uint32_t pad[5];
 };
 static_assert(sizeof(TriRec) == 128, "TriRec must stay 128 bytes");
+static_assert(offsetof(TriRec, bx0) == 48 && offsetof(TriRec, scene) == 88 && offsetof(TriRec, v) == 96,
+              "load_rec reads the record by 16-byte words");
+
+// The 16-byte words of record *p that `words` selects (bit k: word k) as a
+// local TriRec, one vector load each instead of a load per field: rows and
+// pixels of one primitive share it, so the loads hit L1 and what limits them
+// is their count.  Unselected fields are left unset.
+EUC_DEV TriRec load_rec(const TriRec *__restrict__ p, uint32_t words) {
+    const uint4 *q = reinterpret_cast<const uint4 *>(p);
+    uint4 w[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) w[k] = (words >> k) & 1u ? __ldg(q + k) : make_uint4(0u, 0u, 0u, 0u);
+    TriRec r;
+    r.o[0] = __uint_as_float(w[0].x); r.o[1] = __uint_as_float(w[0].y); r.o[2] = __uint_as_float(w[0].z);
+    r.dx[0] = __uint_as_float(w[0].w); r.dx[1] = __uint_as_float(w[1].x); r.dx[2] = __uint_as_float(w[1].y);
+    r.dy[0] = __uint_as_float(w[1].z); r.dy[1] = __uint_as_float(w[1].w); r.dy[2] = __uint_as_float(w[2].x);
+    r.zc[0] = __uint_as_float(w[2].y); r.zc[1] = __uint_as_float(w[2].z); r.zc[2] = __uint_as_float(w[2].w);
+    r.bx0 = w[3].x; r.bx1 = w[3].y; r.by0 = w[3].z; r.by1 = w[3].w;
+    r.vby[0] = __uint_as_float(w[4].x); r.vby[1] = __uint_as_float(w[4].y);
+    r.vby[2] = __uint_as_float(w[4].z); r.vby[3] = __uint_as_float(w[4].w);
+    r.vby[4] = __uint_as_float(w[5].x); r.vby[5] = __uint_as_float(w[5].y);
+    r.scene = w[5].z; r.flags = w[5].w;
+    r.v[0] = w[6].x; r.v[1] = w[6].y; r.v[2] = w[6].z; r.pad[0] = w[6].w;
+    r.pad[1] = w[7].x; r.pad[2] = w[7].y; r.pad[3] = w[7].z; r.pad[4] = w[7].w;
+    return r;
+}
+constexpr uint32_t kRecRaster = 0x3Fu;  // words 0-5: weights, z, bbox, vertices by y, scene, flags
+constexpr uint32_t kRecShade = 0x47u;   // words 0-2 and 6: weights, z, vertex ids
+constexpr uint32_t kRecAll = 0xFFu;
 
 struct SceneStats {
     unsigned long long culled;
@@ -1146,9 +1178,10 @@ __global__ void __launch_bounds__(kBlock, 4) k_raster(const SceneDev *__restrict
             const uint64_t i = i0 + lane;
             if (i >= nitems) continue;
             const uint32_t t = live_tri[l0 + a];
-            const TriRec &r = recs[t];
+            TriRec r = load_rec(recs + t, kRecRaster);
             const uint32_t scene = r.scene;
             if (err[scene]) continue;
+            if (sc[scene].prim != EUC_PRIM_TRIANGLE_LIST) r = load_rec(recs + t, kRecAll);  // a line's walk state
             if (phase == 1 && sc[scene].keytype != KEY_ORDERED) continue;  // the fill pass is for ordered scenes
             uint32_t cnt = 0;
             raster_row(sc[scene], r, t, r.by0 + (uint32_t)(i - off[a]), vbuf, cnt, phase, frags, probe);
@@ -1401,7 +1434,7 @@ EUC_DEV void resolve_direct_chunk(const SceneDev &s, const uint4 &cv, uint64_t l
         if constexpr (F::kDirect) {
             const typename F::U &u = *reinterpret_cast<const typename F::U *>(s.uniforms);
             const float *vb = vdata + (s.geom ? s.gvd_base : s.vd_base);
-            const TriRec &r = recs[t];
+            const TriRec r = load_rec(recs + t, s.prim == EUC_PRIM_TRIANGLE_LIST ? kRecShade : kRecAll);
             float vd[F::NV], frag[F::NF];
             vdata_at<F>(s, r, vb, (float)x, (float)y, vd);
             F::fragment(u, vd, frag);
@@ -1498,7 +1531,7 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
     const uint32_t L = s.level;
     for (uint32_t j = tid; j < njobs; j += kBlock) {
         const int slot = s_job[j] >> 2, c = s_job[j] & 3;
-        const TriRec &r = recs[s_t[slot]];
+        const TriRec &r = recs[s_t[slot]];  // (field loads here: the vector copy costs this path registers)
         float xf, yf;
         if (L == 0) {
             xf = (float)s_xy[slot][0];
@@ -1809,7 +1842,8 @@ __global__ void __launch_bounds__(kBlock) k_resolve_ordered(const SceneDev *__re
         if (s.depth_write) D = z;
         if (!s.pixel_write) continue;
         float frag[F::NF];
-        shade_at<F>(s, u, recs[best], vb, x, y, frag);
+        shade_at<F>(s, u, load_rec(recs + best, s.prim == EUC_PRIM_TRIANGLE_LIST ? kRecShade : kRecAll), vb, x, y,
+                    frag);
         float c[4] = {frag[0], F::NF > 1 ? frag[F::NF > 1 ? 1 : 0] : 0.0f, F::NF > 2 ? frag[F::NF > 2 ? 2 : 0] : 0.0f,
                       F::NF > 3 ? frag[F::NF > 3 ? 3 : 0] : 0.0f};
         if (s.blend == EUC_BLEND_ALPHA) {  // src-over on the unpacked old pixel
