@@ -42,11 +42,11 @@ constexpr int kBlock = 256;           // threads per block in every kernel
 constexpr int kScanPer = 8;           // primitives per thread in the scan
 constexpr int kScanBlock = kBlock * kScanPer;
 
-// VertexData floats per vertex in vdata[]: more than four are padded to a
-// multiple of four, so that their gathers in the resolve are 16-byte loads;
-// up to four are stored as they are (padding three to four costs more in
-// traffic than it saves in loads).
-__host__ __device__ constexpr int vd_stride(int nv) { return nv <= 4 ? nv : (nv + 3) & ~3; }
+// VertexData floats per vertex in vdata[]: three are padded to four, and more
+// than four to a multiple of four, so that a vertex's outputs are whole
+// 16-byte loads in the resolve (whose loads, L1 hits mostly, are what limits
+// it); one, two and four are stored as they are.
+__host__ __device__ constexpr int vd_stride(int nv) { return nv == 3 ? 4 : nv <= 4 ? nv : (nv + 3) & ~3; }
 
 template <class F>
 EUC_DEV void load_vd(const float *__restrict__ p, float out[vd_stride(F::NV)]) {
@@ -60,6 +60,10 @@ EUC_DEV void load_vd(const float *__restrict__ p, float out[vd_stride(F::NV)]) {
             out[i + 2] = q.z;
             out[i + 3] = q.w;
         }
+    } else if constexpr (S == 2) {  // 8-byte aligned: scene regions are 16-byte aligned
+        const float2 q = __ldg(reinterpret_cast<const float2 *>(p));
+        out[0] = q.x;
+        out[1] = q.y;
     } else {
 #pragma unroll
         for (int i = 0; i < S; ++i) out[i] = p[i];
@@ -75,6 +79,8 @@ EUC_DEV void store_vd(float *__restrict__ p, const float *v) {
             *reinterpret_cast<float4 *>(p + i) = make_float4(i < F::NV ? v[i] : 0.0f, i + 1 < F::NV ? v[i + 1] : 0.0f,
                                                              i + 2 < F::NV ? v[i + 2] : 0.0f,
                                                              i + 3 < F::NV ? v[i + 3] : 0.0f);
+    } else if constexpr (S == 2) {
+        *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]);
     } else {
 #pragma unroll
         for (int i = 0; i < S; ++i) p[i] = v[i];
