@@ -573,8 +573,11 @@ def run_serve(args):
         pool.append(r)
         keep.append(kp)
     arr = (abi.ServerRequest * len(pool))(*pool)
-    for _ in range(max(args.warmup, 3)):  # sizes every slot's scratch
-        srv.submit(arr)
+    for _ in range(max(args.warmup, 3)):
+        # enough at once that every slot takes full batches: each slot's
+        # scratch is sized before the timed runs
+        for _ in range(max(args.slots, 1)):
+            srv.submit(arr)
         srv.drain()
         while len(srv.poll(8192)):
             pass
