@@ -521,7 +521,9 @@ def run_gpu(args):
             "roofline": {"bound": "hbm", "kernel": "k_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": alg_bytes,
-                         "traffic": traffic.get(args.workload, {}).get("k_" + dom) if traffic else None},
+                         # captured at the default workload sizes only
+                         "traffic": traffic.get(args.workload, {}).get("k_" + dom)
+                         if traffic and not args.frames and args.scenes == N_SCENES else None},
             # the whole step (every stage, launch gaps included) against the same peak
             "pipeline_roofline": {"achieved": alg_bytes / (ms_step / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                                   "frac": alg_bytes / (ms_step / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
