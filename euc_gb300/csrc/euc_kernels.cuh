@@ -530,6 +530,13 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
                                                   uint32_t *__restrict__ rows, uint2 *__restrict__ chunk_sums,
                                                   int *__restrict__ err, SceneStats *__restrict__ stats,
                                                   uint4 *__restrict__ cov, const uint8_t *__restrict__ galive) {
+    // a warp's 32 records, staged so that they leave as 512-byte stores;
+    // 16-byte word k of lane l's record sits at l * 8 + (k ^ (l & 7)), which
+    // keeps both the staging and the copy-out at the minimum four wavefronts
+    __shared__ uint4 s_rec[kBlock / 32][32 * 8];
+    const int lane = threadIdx.x & 31;
+    uint4 *stage = s_rec[threadIdx.x >> 5];
+    bool staged = false;
     const uint64_t t = (uint64_t)blockIdx.x * kBlock + threadIdx.x;
     const int si = chunk_scene ? (int)chunk_scene[blockIdx.x] : 0;
     const SceneDev &s = sc[si];
@@ -707,15 +714,27 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
                 if (nrows) {
                     // only a primitive with rows is ever read again (the scan
                     // keeps exactly those)
-                    const float4 *src = reinterpret_cast<const float4 *>(&r);
-                    float4 *dst = reinterpret_cast<float4 *>(recs + t);
+                    const uint4 *src = reinterpret_cast<const uint4 *>(&r);
 #pragma unroll
-                    for (int k = 0; k < 8; ++k) dst[k] = src[k];
+                    for (int k = 0; k < 8; ++k) stage[lane * 8 + (k ^ (lane & 7))] = src[k];
+                    staged = true;
                     cx0 = bx0;
                     cx1 = bx1;
                     cy0 = by0;
                     cy1 = by1;
                 }
+            }
+        }
+    }
+    {  // the warp's staged records, 16-byte word c of the warp's 4 KB per lane and pass
+        const uint32_t live = __ballot_sync(0xFFFFFFFFu, staged);
+        __syncwarp();
+        if (live) {
+            uint4 *dst = reinterpret_cast<uint4 *>(recs + (t - (uint64_t)lane));
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int c = k * 32 + lane, owner = c >> 3;
+                if ((live >> owner) & 1u) dst[c] = stage[owner * 8 + ((c & 7) ^ (owner & 7))];
             }
         }
     }
