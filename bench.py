@@ -592,6 +592,7 @@ def run_serve(args):
     runs = []
     clocks = ClockSampler(bus)
     clocks.start()
+    time.sleep(1.0)  # the sampler's start (NVML set-up) stays out of the first run
     for i, rate in enumerate(float(r) for r in args.rates.split(",")):
         _, summ = serve.run_poisson(srv, arr, outs, rate, args.serve_seconds, seed=args.seed + 17 * i + rank)
         summ.pop("stats")
