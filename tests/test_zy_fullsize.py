@@ -4,7 +4,8 @@ The oracle renders these in about a second on the host's cores, so the GPU
 output is compared with it directly, not only through size-independent
 properties: the 1080p 200k-triangle soup, the two-pass 500k-triangle knot
 (2048^2 shadow map, 1080p MSAA colour) and the 256-scene batch, plus the
-property that the batch equals its scenes rendered one at a time.  Depth is
+property that the batch equals its scenes rendered one at a time, and a
+16384^2 target for the index arithmetic of large targets.  Depth is
 bit-exact and candidate counts exact; colour is exact except under Phong
 (+-1 LSB, powf).  This file sorts late: its cases are the slowest.
 """
@@ -58,3 +59,25 @@ def test_full_batch_matches_oracle_and_per_scene(gpu_ctx):
     for f, b in zip(specs, batched):
         ref, _ = run_oracle(f, threads=threads)
         assert_targets_match(f, ref, b, color_tol=_tol(f))
+
+
+def test_large_target_index_arithmetic(gpu_ctx):
+    """A 16384 x 16384 target (2^28 pixels, 4 GB of targets and keys on the
+    device): triangles in its corners reach row offsets beyond 2^31 bytes and
+    key indices beyond 2^27; depth bit-exact, colour exact."""
+    from oracle import oracle
+    big = 16384
+    tris = []
+    for cx, cy in ((-0.9995, -0.9995), (0.9995, 0.9995), (0.9995, -0.9995), (-0.9995, 0.9995)):
+        s = 0.0004
+        tris += [[cx - s, cy - s, 0.25, 1.0], [cx + s, cy - s, 0.5, 1.0], [cx, cy + s, 0.75, 1.0]]
+    cols = [[255, 0, 0, 255], [0, 255, 0, 255], [0, 0, 255, 255]] * 4
+    frame = scenes.clip_triangles_frame(tris, cols, big, big, pixel_fmt=abi.FMT_RGBA8)
+    ref, ref_stats = run_oracle(frame, threads=oracle.hw_threads())
+    got, got_stats = run_gpu(gpu_ctx, frame)
+    assert got_stats[0][0] == abi.OK
+    assert got_stats[0][1] == ref_stats[0][1] and ref_stats[0][1] > 4 * 10
+    # the drawn corners lie in both halves of the 2^31-byte row range
+    ys = np.nonzero(ref["depth"] < 1.0)[0]
+    assert ys.min() < 64 and ys.max() > big - 64
+    assert_targets_match(frame, ref, got)
