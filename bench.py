@@ -93,6 +93,15 @@ def dist_env():
     return replicas.dist_env()
 
 
+def run_config(args, specs, world):
+    """The `config` of a bench line; both arms print the same one."""
+    alg_bytes = sum(f.algorithmic_bytes() for f in specs)
+    keys = 8 * sum(t.width * t.height for f in specs for t in f.targets if t.fmt != 4)
+    return {"workload": WORKLOADS[args.workload][0], "name": args.workload, "scenes": args.scenes, "seed": args.seed,
+            "l2": "no flush: %.0f MB of inputs and targets per step > 129 MB L2" % ((alg_bytes + keys) / 1e6),
+            "parallelism": "replicas" if world > 1 else "1 GPU"}
+
+
 def make_frames(args, rank):
     from euc_gb300 import replicas, scenes
     seed = replicas.replica_seed(args.seed, rank)
@@ -204,7 +213,7 @@ def run_reference(args):
            "unit": unit, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": 1e3 * total_t / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators)",
-           "config": {"workload": desc, "name": args.workload, "scenes": args.scenes, "seed": args.seed},
+           "config": run_config(args, frames, world),
            "cpu_baseline": {"value": v, "unit": unit, "cores": threads, "kind": "port",
                             "sample": "%d scenes (rotating through the %d) in %.1f s" % (total_n, len(frames), total_t)},
            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -504,10 +513,7 @@ def run_gpu(args):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generators), resident in HBM",
-            "config": {"workload": desc, "name": args.workload, "scenes": args.scenes, "seed": args.seed,
-                       "l2": "no flush: %.0f MB of inputs and targets per step > 129 MB L2" % (
-                           (alg_bytes + 8 * sum(t.width * t.height for f in specs for t in f.targets if t.fmt != 4)) / 1e6),
-                       "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "config": run_config(args, specs, world),
             "form": {"timed": "euc_graph replay" if form == "graph" else "euc_render_batch calls",
                      "plain_value": world * args.scenes / (ms_plain / args.steps / 1e3),
                      "graph_value": world * args.scenes / (ms_graph / args.steps / 1e3) if ms_graph else None,

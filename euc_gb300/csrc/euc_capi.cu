@@ -6,6 +6,7 @@
 // on demand (euc_ctx_reserve pre-sizes them).  Scene tables and uniforms go
 // up through a ring of pinned staging slots, each guarded by an event.
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -1317,9 +1318,12 @@ int euc_render_host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int t
 // g_noalloc_scratch (kNaBytes, about 21.0 MiB).  Every GPU that loads this
 // library holds that array until the process exits.
 //
-// Limits: at most kNaMaxVerts vertices, kNaMaxGroups primitives (index
-// triples), kNaMaxPixels target pixels; larger scenes are rejected with
-// EUC_ERR_CAPACITY before anything is enqueued.
+// Limits: at most kNaMaxVerts vertices, kNaMaxGroups primitive slots (one
+// per triangle, one per line, three per triangle of a LineTriangleList) and
+// kNaMaxPixels target pixels; larger scenes are rejected with
+// EUC_ERR_CAPACITY before anything is enqueued.  The scene table and the
+// uniforms reach the device as a kernel parameter, so nothing of the
+// caller's host memory is read once the call has returned.
 //
 // Every call uses the same array and leaves its contents behind for the next
 // call.  Each call clears on its stream the parts that must start at zero
@@ -1328,8 +1332,10 @@ int euc_render_host_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, int t
 // the array and corrupt each other's results: issue them on one stream.
 //
 // Set-up: the first call on a device looks up the array's device address for
-// that device (cudaGetSymbolAddress, with that device current) and caches it.
-// That first call should come before any stream capture begins.
+// that device (cudaGetSymbolAddress, with that device current) and caches it
+// with the CUDA context it was found in; a call in another context (after
+// cudaDeviceReset) looks it up again.  The first call on a device, and the
+// first after a reset, should come before any stream capture begins.
 // ===========================================================================
 namespace {
 
@@ -1362,6 +1368,7 @@ static_assert(kNaMaxVerts % kBlock == 0 && kNaMaxGroups % kBlock == 0 && kNaMaxP
 constexpr int kNaMaxDevices = 64;
 std::mutex g_na_mu;
 unsigned char *g_na_ptr[kNaMaxDevices];
+CUcontext g_na_ctx[kNaMaxDevices];  // the context each address was looked up in
 int g_na_nsm[kNaMaxDevices];
 
 }  // namespace
@@ -1370,10 +1377,32 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
 namespace {
 
-// Device address of g_noalloc_scratch on the current device (looked up once).
+// The driver's cuCtxGetCurrent, found through the runtime (no link to the
+// driver library); nullptr when the driver does not offer it.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+CtxGetCurrentFn ctx_get_current() {
+    static CtxGetCurrentFn fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            (void)cudaGetLastError();
+            f = nullptr;
+        }
+        return (CtxGetCurrentFn)f;
+    }();
+    return fn;
+}
+
+// Device address of g_noalloc_scratch on the current device: looked up once
+// per device and context, so that after a cudaDeviceReset (a new primary
+// context, the module loaded again) it is looked up again.
 int na_scratch(int dev, unsigned char **ptr, int *nsm) {
+    CUcontext cur = nullptr;
+    if (CtxGetCurrentFn f = ctx_get_current())
+        if (f(&cur) != CUDA_SUCCESS) cur = nullptr;
     std::lock_guard<std::mutex> g(g_na_mu);
-    if (!g_na_ptr[dev]) {
+    if (!g_na_ptr[dev] || g_na_ctx[dev] != cur) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
@@ -1387,6 +1416,7 @@ int na_scratch(int dev, unsigned char **ptr, int *nsm) {
             return EUC_ERR_CUDA;
         }
         g_na_ptr[dev] = (unsigned char *)p;
+        g_na_ctx[dev] = cur;
         g_na_nsm[dev] = n;
     }
     *ptr = g_na_ptr[dev];
@@ -1395,6 +1425,26 @@ int na_scratch(int dev, unsigned char **ptr, int *nsm) {
 }
 
 thread_local int t_na_nsm = 1;  // SM count of the device of the current call
+
+// A call's scene table, zero bases and uniforms, handed to the device as a
+// kernel parameter (no host memory is read after the call returns).
+struct NaStage {
+    SceneDev d;
+    uint64_t zero[6];             // the vertex / primitive / pixel bases of one scene
+    alignas(16) unsigned char uni[512];
+};
+static_assert(sizeof(euc_phong_uniforms) <= sizeof(NaStage::uni), "uniform copies hold any shader's struct");
+
+// Writes the stage into the scratch array: the scene at 0, the zero bases at
+// `off_b`, the uniforms at `off_u` (`usize` bytes).
+__global__ void k_na_stage(const NaStage st, unsigned char *__restrict__ a, uint32_t off_b, uint32_t off_u,
+                           uint32_t usize) {
+    const unsigned char *d = reinterpret_cast<const unsigned char *>(&st.d);
+    for (uint32_t i = threadIdx.x; i < sizeof(SceneDev); i += blockDim.x) a[i] = d[i];
+    const unsigned char *z = reinterpret_cast<const unsigned char *>(st.zero);
+    for (uint32_t i = threadIdx.x; i < sizeof(st.zero); i += blockDim.x) a[off_b + i] = z[i];
+    for (uint32_t i = threadIdx.x; i < usize; i += blockDim.x) a[off_u + i] = st.uni[i];
+}
 
 template <class F>
 void na_vertex_resolve(bool vertex, const SceneDev *sc, const uint64_t *base, uint64_t nblk, unsigned char *a,
@@ -1464,19 +1514,20 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
     const uint64_t vtx = pad_up(p.d.nverts, kBlock);
     const uint64_t tri = pad_up(std::max<uint64_t>(p.d.ngroups, 1), kBlock);
     const uint64_t pix = pad_up((uint64_t)p.d.W * p.d.H, kBlock);
-    // scene table | vtx base | tri base | pix base | uniforms, staged on the host stack
+    // scene table | vtx base | tri base | pix base | uniforms, written by a
+    // kernel from its parameter
     const size_t off_b = pad_up(sizeof(SceneDev), 16);
     const size_t off_u = off_b + 3 * 16;
-    alignas(16) unsigned char stage[kNaStage];
     static_assert((sizeof(SceneDev) + 15) / 16 * 16 + 3 * 16 + sizeof(euc_phong_uniforms) <= kNaStage,
                   "staging area too small");
-    SceneDev d = p.d;
+    NaStage stage;
+    std::memset(&stage, 0, sizeof(stage));
+    SceneDev &d = stage.d;
+    d = p.d;
     d.vtx_base = d.vd_base = d.tri_base = d.pix_base = 0;
     d.uniforms = a + off_u;
-    std::memset(stage, 0, off_u);
-    std::memcpy(stage, &d, sizeof(d));
-    std::memcpy(stage + off_u, p.uniforms, p.usize);
-    CUDA_TRY(cudaMemcpyAsync(a, stage, off_u + p.usize, cudaMemcpyHostToDevice, st));
+    std::memcpy(stage.uni, p.uniforms, p.usize);
+    k_na_stage<<<1, 128, 0, st>>>(stage, a, (uint32_t)off_b, (uint32_t)off_u, (uint32_t)p.usize);
     const SceneDev *dsc = (const SceneDev *)a;
     const uint64_t *zero_base = (const uint64_t *)(a + off_b);  // every base is 0 for a single scene
     k_prep<<<(unsigned)((tri / kBlock + kBlock - 1) / kBlock), kBlock, 0, st>>>(

@@ -412,16 +412,19 @@ int euc_sample_nearest(const void *texels, uint32_t ndim, const uint32_t *size, 
  * thread that cannot pay for cudaMalloc/cudaFree (both synchronise the whole
  * device).  Scratch lives in one fixed array inside the library (about 21.0
  * MiB per device that loads it, held until exit).  Limits: 65,536 vertices,
- * 65,536 primitives (index triples), 1,048,576 target pixels; larger scenes
- * return EUC_ERR_CAPACITY, and so do order-dependent blends (EUC_BLEND_ALPHA,
+ * 65,536 primitive slots (one per triangle, one per line, three per triangle
+ * of a LineTriangleList), 1,048,576 target pixels; larger scenes return
+ * EUC_ERR_CAPACITY, and so do order-dependent blends (EUC_BLEND_ALPHA,
  * EUC_FLAG_ORDERED), whose fragment lists are sized on the device, and
  * geometry stages, whose output vertices need room beyond the fixed array.  Runs on
  * the current device, ordered on `stream`.
  * `device_status` (nullable, device memory) receives EUC_OK or
  * EUC_ERR_INDEX_OOB once the render has run.  All calls share the scratch
  * array: calls whose work overlaps on the GPU race, so issue them on one
- * stream.  The first call on a device looks up the array's device address;
- * make it before any stream capture starts.                                 */
+ * stream.  The first call on a device (and the first after cudaDeviceReset)
+ * looks up the array's device address; make it before any stream capture
+ * starts.  The scene table and uniforms travel as a kernel parameter: no
+ * host memory is read after the call returns.                               */
 int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uniforms, size_t uniforms_size,
                        const euc_vertex_layout *layout, const void *vertices, size_t nverts,
                        const uint32_t *indices, size_t nindices, const euc_target *pixel,

@@ -1,5 +1,6 @@
 """Known answers derived by hand from euc's Rust semantics, checked against the
-CPU oracle (and, where the same scene runs on the GPU, in test_gpu_kat.py).
+CPU oracle.  The GPU path is held to the oracle on the same modes in
+test_gpu_parity.py and test_gpu_errors.py.
 
 Each expected value is worked out in the comment beside it from the cited
 euc source lines, not from running any restatement.

@@ -5,7 +5,7 @@ synchronisation of cudaMalloc/cudaFree).
 
 It is checked through the C ABI against euc_render on the same inputs, twice
 in a row, because every call reuses the library's one scratch array and must
-not see the previous call's leftovers.  This file sorts last so that a run
+not see the previous call's leftovers, and against the CPU oracle directly.  This file sorts last so that a run
 stopping at the first failure has already run every other test.
 """
 import ctypes as C
@@ -15,6 +15,7 @@ import pytest
 
 from euc_gb300 import abi, capi, frames, scenes
 from frameutil import assert_targets_match
+from oracle import oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -42,6 +43,9 @@ CASES = {
     "soup320x180": lambda: scenes.soup_frame(seed=1, width=320, height=180, ntris=4000, area_hi=3000.0),
     "knot_shadow_msaa": lambda: scenes.knot_frame(seed=2, width=320, height=180, shadow_size=256, tubular=180,
                                                   radial=20, tex_size=64, aa_level=1),
+    # line primitives: one slot per line, three per triangle of a LineTriangleList
+    "lines320x180": lambda: scenes.lines_frame(seed=4, width=320, height=180, nlines=3000),
+    "wireframe320x240": lambda: scenes.wireframe_frame(seed=5, width=320, height=240, lon=24, lat=12),
 }
 
 
@@ -59,6 +63,8 @@ def test_noalloc_matches_render_on_two_calls(name):
         ref = ref_df.to_host()
     finally:
         ctx.close()
+    oref, _, codes = oracle.run_frame(frame)
+    assert all(c == abi.OK for c in codes)
     status = torch.full((1,), -1, dtype=torch.int32, device="cuda:0")
     for call in range(2):
         df = frames.DeviceFrame(frame, "cuda:0")
@@ -67,7 +73,9 @@ def test_noalloc_matches_render_on_two_calls(name):
         _render_noalloc(df, status)
         torch.cuda.synchronize()
         assert int(status.item()) == abi.OK, "call %d" % call
-        assert_targets_match(frame, ref, df.to_host(), color_tol=tol)
+        got = df.to_host()
+        assert_targets_match(frame, ref, got, color_tol=tol)
+        assert_targets_match(frame, oref, got, color_tol=tol)
 
 
 def test_noalloc_rejects_scenes_beyond_its_limits():
