@@ -5,7 +5,7 @@ the struct sizes against the C compiler's.
 """
 import ctypes as C
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 # status codes
 OK = 0
@@ -125,7 +125,7 @@ class Stats(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("raster_blocks_per_sm", C.c_uint32), ("raster_warp_rows", C.c_uint32),
                 ("chunk_group", C.c_uint32), ("chunk_blocks_per_sm", C.c_uint32), ("raster_probe", C.c_uint32),
-                ("host_copy", C.c_uint32)]
+                ("host_copy", C.c_uint32), ("strip_path", C.c_uint32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

@@ -1,14 +1,15 @@
 """Launch-shape autotuner for batched renders.
 
-`euc_ctx_set_tuning` changes how a batch is spread over the GPU: persistent
-raster blocks per SM, the (primitive, row) items a raster warp claims at a
-time, whether the raster reads a key before its atomicMin, and the chunk
-grouping and grid cap of the init/resolve kernels.  None of these changes a
-result.  The tuner times a `frames.DeviceBatch` under a set
-of candidate shapes (coordinate descent: the raster knobs first, then the
-chunk knobs), checks that every candidate's targets are byte-identical to the
-default shape's, keeps the fastest and caches the choice per device and
-workload signature in a JSON file next to the built library.
+`euc_ctx_set_tuning` changes how a batch is spread over the GPU: which
+scenes go to the shared-memory strips, persistent raster blocks per SM, the
+(primitive, row) items a raster warp claims at a time, whether the raster
+reads a key before its atomicMin, and the chunk grouping and grid cap of the
+init/resolve kernels.  None of these changes a result.  The tuner times a
+`frames.DeviceBatch` under a set of candidate shapes (coordinate descent: the
+strip path, then the raster knobs, then the chunk knobs), checks that every
+candidate's targets are byte-identical to the default shape's, keeps the
+fastest and caches the choice per device, library build and workload
+signature in a JSON file next to the built library.
 """
 import json
 import os
@@ -26,13 +27,18 @@ RASTER_WARP_ROWS = (256, 128, 64)
 CHUNK_GROUP = (0, 1, 4, 16)        # 0: adaptive
 CHUNK_BLOCKS = (0, 8, 32)          # 0: 16 per SM
 RASTER_PROBE = (0, 1)              # 0: atomics only; 1: read keys before their atomics
+STRIP_PATH = (0, 1, 2)             # shared-memory strips: 0 for overdrawn scenes, 1 off, 2 always
 
 
 def workload_key(batch):
     """Device name, SM count and the batch's shape: scenes, primitives,
     target pixels and shader kinds per pass."""
     props = torch.cuda.get_device_properties(batch.color.device)
-    parts = [props.name.replace(" ", "_"), str(props.multi_processor_count)]
+    try:
+        build = "%d" % int(os.path.getmtime(_build.LIB))
+    except OSError:
+        build = "?"
+    parts = [props.name.replace(" ", "_"), str(props.multi_processor_count), "lib" + build]
     for arr in batch.scene_arrays():
         tris = sum(s.nindices // 3 for s in arr)
         pix = sum(max(s.pixel.width * s.pixel.height, s.depth.width * s.depth.height) for s in arr)
@@ -97,6 +103,11 @@ def tune(ctx, batch, stream=None, reps=5, cache=CACHE, verify=True, log=None):
 
     best = {k: 0 for k, _ in abi.Tuning._fields_}
     default_ms = best_ms = run(best)
+    for sp in STRIP_PATH:
+        cand = dict(best, strip_path=sp)
+        ms = run(cand)
+        if ms < best_ms:
+            best, best_ms = cand, ms
     for pr in RASTER_PROBE:
         for rb in RASTER_BLOCKS:
             for wr in RASTER_WARP_ROWS:

@@ -51,6 +51,9 @@ struct euc_ctx {
     DevBuf obsum, frags;  // ordered path: pixel-scan block sums, fragment lists
     DevBuf plan;          // plan_chunks: k_init and k_resolve chunk bases (2 x (scenes + 1))
     DevBuf galive;        // geometry stage: 1 per output slot that holds a triangle
+    // strip path: per-strip entry counts, fill cursors, list offsets, unit
+    // offsets, the entry lists and the strip of each unit
+    DevBuf strip_cnt, strip_fill, strip_off, strip_uoff, entries, unit_strip;
     int raster_blocks = 0;  // resident k_raster blocks per SM
     bool pageable = false;  // kernels may access pageable host memory (cudaDevAttrPageableMemoryAccess)
     euc_tuning tune{};      // launch-shape overrides (0 = default)
@@ -511,6 +514,30 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
         pix += pad_up((uint64_t)p.d.W * p.d.H, kBlock);
         res += resolve_blocks(p.d);
     }
+    // strip path: the scenes it may take, their strips, and the widest
+    // strip's keys (k_strip's dynamic shared memory).  In the default mode a
+    // scene with fewer than one primitive per kStripMinPixels target pixels
+    // cannot be overdrawn enough to pay for the strip launches; k_bin_count
+    // decides for the others on the device.
+    std::vector<uint64_t> strip_first(ns + 1);
+    uint64_t nstrips = 0;
+    size_t strip_smem = 0;
+    const uint32_t strip_mode = ctx->tune.strip_path;
+    for (int i = 0; i < ns; ++i) {
+        Plan &p = plans[i];
+        strip_first[i] = nstrips;
+        const bool can = p.d.prim == EUC_PRIM_TRIANGLE_LIST && p.d.keytype != KEY_ORDERED &&
+                         (strip_mode == 2 ||
+                          (strip_mode == 0 && (uint64_t)p.d.ntris * kStripMinPixels >= (uint64_t)p.d.W * p.d.H));
+        const uint32_t h = can ? strip_rows(p.d.W, p.d.H) : 0u;
+        p.d.strip_h = h;
+        p.d.strip_base = (uint32_t)nstrips;
+        p.d.nstrips = h ? (p.d.H + h - 1) / h : 0u;
+        nstrips += p.d.nstrips;
+        if (h) strip_smem = std::max(strip_smem, (size_t)h * strip_pitch(p.d.W) * sizeof(unsigned long long));
+    }
+    strip_first[ns] = nstrips;
+    if (nstrips >= 0x7FFFFFFFull) return EUC_ERR_CAPACITY;
     // geometry stage: its input threads, and its output vertices after every
     // scene's vertex-stage outputs (the vertex launches cover only those)
     const uint64_t vtx_stage = vtx;  // the vertex launches end here
@@ -544,13 +571,25 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
     if ((rc = grow(ctx->cov, ns * sizeof(uint4)))) return rc;
     if ((rc = grow(ctx->plan, 2 * (ns + 1) * sizeof(uint64_t)))) return rc;
     if (gin && (rc = grow(ctx->galive, tri))) return rc;
+    // strip lists: an admitted primitive has one entry per strip it overlaps;
+    // k_bin_count admits primitives while the list has room
+    const uint64_t entry_cap = nstrips ? 2 * tri + (1ull << 21) : 0;
+    if (nstrips) {
+        if ((rc = grow(ctx->strip_cnt, nstrips * sizeof(uint32_t)))) return rc;
+        if ((rc = grow(ctx->strip_fill, nstrips * sizeof(uint32_t)))) return rc;
+        if ((rc = grow(ctx->strip_off, (nstrips + 1) * sizeof(uint32_t)))) return rc;
+        if ((rc = grow(ctx->strip_uoff, (nstrips + 1) * sizeof(uint32_t)))) return rc;
+        if ((rc = grow(ctx->entries, entry_cap * sizeof(uint2)))) return rc;
+        if ((rc = grow(ctx->unit_strip, (nstrips + entry_cap / kStripUnit + 1) * sizeof(uint32_t)))) return rc;
+    }
     // staging: scene table | vtx bases | resolve bases | geometry bases |
-    // scene of each setup chunk | uniforms
+    // first strip of each scene | scene of each setup chunk | uniforms
     const size_t off_sc = 0;
     const size_t off_vb = pad_up(ns * sizeof(SceneDev), 16);
     const size_t off_rb = off_vb + pad_up(ns * sizeof(uint64_t), 16);
     const size_t off_gb = off_rb + pad_up(ns * sizeof(uint64_t), 16);
-    const size_t off_cs = off_gb + pad_up(ns * sizeof(uint64_t), 16);
+    const size_t off_sb = off_gb + pad_up(ns * sizeof(uint64_t), 16);
+    const size_t off_cs = off_sb + pad_up((ns + 1) * sizeof(uint64_t), 16);
     size_t off_u = off_cs + pad_up(nchunks * sizeof(uint32_t), 16);
     std::vector<size_t> uoff(ns);
     for (int i = 0; i < ns; ++i) {
@@ -571,6 +610,7 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
     uint8_t *dv = (uint8_t *)(so ? so->dev : slot->dev);
     SceneDev *hsc = (SceneDev *)(h + off_sc);
     uint64_t *hvb = (uint64_t *)(h + off_vb), *hrb = (uint64_t *)(h + off_rb), *hgb = (uint64_t *)(h + off_gb);
+    std::memcpy(h + off_sb, strip_first.data(), (ns + 1) * sizeof(uint64_t));
     uint32_t *hcs = (uint32_t *)(h + off_cs);
     for (int i = 0; i < ns; ++i) {  // scene ranges of primitives are padded to whole setup chunks
         const uint64_t c0 = plans[i].d.tri_base / kBlock, c1 = (i + 1 < ns ? plans[i + 1].d.tri_base : tri) / kBlock;
@@ -587,9 +627,13 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
     CUDA_TRY(cudaMemcpyAsync(dv, h, off_u, cudaMemcpyHostToDevice, st));
     const SceneDev *dsc = (const SceneDev *)(dv + off_sc);
     const uint64_t *dvb = (const uint64_t *)(dv + off_vb), *drb = (const uint64_t *)(dv + off_rb),
-                   *dgb = (const uint64_t *)(dv + off_gb);
-    k_prep<<<(unsigned)((std::max<uint64_t>((uint64_t)ns, nchunks) + kBlock - 1) / kBlock), kBlock, 0, st>>>(
-        (int *)ctx->err.p, (SceneStats *)ctx->stats.p, (uint4 *)ctx->cov.p, ns, (uint2 *)ctx->chunk_sums.p, nchunks);
+                   *dgb = (const uint64_t *)(dv + off_gb), *dsb = (const uint64_t *)(dv + off_sb);
+    const uint32_t *dcs = (const uint32_t *)(dv + off_cs);
+    const uint64_t nprep = std::max<uint64_t>(std::max<uint64_t>((uint64_t)ns, nchunks), std::max<uint64_t>(nstrips, 2));
+    k_prep<<<(unsigned)((nprep + kBlock - 1) / kBlock), kBlock, 0, st>>>(
+        (int *)ctx->err.p, (SceneStats *)ctx->stats.p, (uint4 *)ctx->cov.p, ns, (uint2 *)ctx->chunk_sums.p, nchunks,
+        (uint32_t *)ctx->strip_cnt.p, (uint32_t *)ctx->strip_fill.p, (uint32_t)nstrips,
+        (unsigned long long *)ctx->totals.p);
     // vertex stage, one launch per shader kind
     cudaEvent_t e0 = prof_event(ctx, st);
     for (int a = 0; a < ns;) {
@@ -613,17 +657,28 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
         a = b;
     }
     cudaEvent_t e1 = prof_event(ctx, st);
-    k_setup<<<(unsigned)nchunks, kBlock, 0, st>>>(dsc, (const uint32_t *)(dv + off_cs), (const float4 *)ctx->clip.p,
+    k_setup<<<(unsigned)nchunks, kBlock, 0, st>>>(dsc, dcs, (const float4 *)ctx->clip.p,
                                                    (TriRec *)ctx->recs.p, (uint32_t *)ctx->rows.p,
                                                    (uint2 *)ctx->chunk_sums.p, (int *)ctx->err.p,
                                                    (SceneStats *)ctx->stats.p, (uint4 *)ctx->cov.p,
                                                    (const uint8_t *)ctx->galive.p);
+    // binning blocks stride the setup chunks
+    const unsigned bin_grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(nchunks, (uint64_t)ctx->nsm * 8));
+    if (nstrips) {  // the strip path's routing and counts
+        k_bin_count<<<bin_grid, kBlock, 0, st>>>(
+            dsc, dcs, nchunks, (uint32_t *)ctx->rows.p, (const TriRec *)ctx->recs.p, (const uint4 *)ctx->cov.p,
+            (const SceneStats *)ctx->stats.p, (uint2 *)ctx->chunk_sums.p, (uint32_t *)ctx->strip_cnt.p,
+            (unsigned long long *)ctx->totals.p + 6, entry_cap, strip_mode);
+        ctx->launches += 1;
+    }
     cudaEvent_t e2 = prof_event(ctx, st);
     uint64_t *const ibase = (uint64_t *)ctx->plan.p, *const rbase = ibase + ns + 1;
-    k_scan_plan<<<(unsigned)nscan + 1, kBlock, 0, st>>>((const uint32_t *)ctx->rows.p, (const uint2 *)ctx->chunk_sums.p,
-                                                        tri, (uint32_t *)ctx->live_tri.p, (uint64_t *)ctx->live_rowoff.p,
-                                                        (unsigned long long *)ctx->totals.p, (uint32_t)nscan, dsc, ns,
-                                                        (const uint4 *)ctx->cov.p, ibase, rbase);
+    const uint64_t nsblk = (nstrips + kScanBlock - 1) / kScanBlock;
+    k_scan_plan<<<(unsigned)(nscan + 1 + nsblk), kBlock, 0, st>>>(
+        (const uint32_t *)ctx->rows.p, (const uint2 *)ctx->chunk_sums.p, tri, (uint32_t *)ctx->live_tri.p,
+        (uint64_t *)ctx->live_rowoff.p, (unsigned long long *)ctx->totals.p, (uint32_t)nscan, dsc, ns,
+        (const uint4 *)ctx->cov.p, ibase, rbase, (const uint32_t *)ctx->strip_cnt.p, (uint32_t)nstrips,
+        (uint32_t *)ctx->strip_off.p, (uint32_t *)ctx->strip_uoff.p, (uint32_t *)ctx->unit_strip.p);
     cudaEvent_t e3 = prof_event(ctx, st);
     const euc_tuning &tu = ctx->tune;
     const uint64_t ichunks = (pix + kInitChunk - 1) / kInitChunk + ns;  // bounds the chunks plan_chunks counts
@@ -631,6 +686,18 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
         dsc, ibase, ns, (const uint4 *)ctx->cov.p, (unsigned long long *)ctx->vbuf.p,
         chunk_group(ichunks, ctx->nsm, tu.chunk_group, tu.chunk_blocks_per_sm));
     cudaEvent_t e4 = prof_event(ctx, st);
+    if (nstrips) {  // the strip lists, then the strips (after k_init, before the item queue)
+        k_bin<<<bin_grid, kBlock, 0, st>>>(dsc, dcs, nchunks, (const uint32_t *)ctx->rows.p, (const TriRec *)ctx->recs.p,
+                                           (const uint4 *)ctx->cov.p, (const SceneStats *)ctx->stats.p,
+                                           (const uint32_t *)ctx->strip_off.p, (uint32_t *)ctx->strip_fill.p,
+                                           (uint2 *)ctx->entries.p, strip_mode);
+        k_strip<<<(unsigned)ctx->nsm * 2, kStripThreads, strip_smem, st>>>(
+            dsc, dsb, ns, (const uint4 *)ctx->cov.p, (const uint32_t *)ctx->strip_off.p,
+            (const uint32_t *)ctx->strip_uoff.p, (const uint32_t *)ctx->unit_strip.p, (const uint2 *)ctx->entries.p,
+            (const TriRec *)ctx->recs.p, (const int *)ctx->err.p, (unsigned long long *)ctx->vbuf.p,
+            (SceneStats *)ctx->stats.p, (unsigned long long *)ctx->totals.p);
+        ctx->launches += 2;
+    }
     const int witems = tu.raster_warp_rows ? (int)tu.raster_warp_rows : kWarpItems;
     // persistent blocks, but no more than the items can keep busy: a
     // primitive slot has at most max(W, H) + 2 items (rows, or line steps)
@@ -742,6 +809,12 @@ int euc_ctx_create(int device, euc_ctx **out) {
         return EUC_ERR_CUDA;
     }
     c->pageable = pageable != 0;
+    // k_strip's keys: up to kStripKeyBytes of dynamic shared memory
+    if (cudaFuncSetAttribute(k_strip, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStripKeyBytes) != cudaSuccess) {
+        (void)cudaGetLastError();
+        delete c;
+        return EUC_ERR_CUDA;
+    }
     *out = c;
     return EUC_OK;
 }
@@ -752,7 +825,8 @@ int euc_ctx_destroy(euc_ctx *ctx) {
     cudaDeviceSynchronize();
     DevBuf *bufs[] = {&ctx->clip, &ctx->vdata, &ctx->recs, &ctx->rows, &ctx->chunk_sums, &ctx->live_tri, &ctx->live_rowoff,
                       &ctx->totals, &ctx->vbuf, &ctx->err, &ctx->stats, &ctx->cov, &ctx->obsum, &ctx->frags,
-                      &ctx->plan, &ctx->galive, &ctx->h_arena, &ctx->h_tex[0]};
+                      &ctx->plan, &ctx->galive, &ctx->h_arena, &ctx->h_tex[0], &ctx->strip_cnt, &ctx->strip_fill,
+                      &ctx->strip_off, &ctx->strip_uoff, &ctx->entries, &ctx->unit_strip};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (ctx->h_pinned.p) cudaFreeHost(ctx->h_pinned.p);
@@ -796,7 +870,8 @@ int euc_ctx_set_tuning(euc_ctx *ctx, const euc_tuning *t) {
         v = *t;
         if (v.raster_warp_rows && (v.raster_warp_rows % 32 || v.raster_warp_rows > (uint32_t)kWarpItems))
             return EUC_ERR_INVALID;
-        if (v.raster_blocks_per_sm > 64 || v.chunk_group > 1024 || v.chunk_blocks_per_sm > 64 || v.raster_probe > 2)
+        if (v.raster_blocks_per_sm > 64 || v.chunk_group > 1024 || v.chunk_blocks_per_sm > 64 || v.raster_probe > 2 ||
+            v.strip_path > 2)
             return EUC_ERR_INVALID;
         if (v.host_copy > EUC_HOST_COPY_DIRECT || (v.host_copy == EUC_HOST_COPY_DIRECT && !ctx->pageable))
             return EUC_ERR_INVALID;
@@ -910,18 +985,19 @@ struct euc_graph {
     cudaGraphExec_t exec = nullptr;
     int nscenes = 0;
     uint64_t launches = 0;   // kernels in the recorded batch
-    void *scratch[14] = {};  // the context's scratch pointers the graph was recorded with
+    void *scratch[20] = {};  // the context's scratch pointers the graph was recorded with
 };
 
 namespace {
 
 // The scratch buffers a recorded batch reads and writes.  A later render that
 // grows one of them moves it, and the graph may then no longer be launched.
-constexpr int kScratchBufs = 14;
+constexpr int kScratchBufs = 20;
 void scratch_ptrs(const euc_ctx *c, void *out[kScratchBufs]) {
-    const DevBuf *b[kScratchBufs] = {&c->clip, &c->vdata,  &c->recs, &c->rows,  &c->chunk_sums,
-                                     &c->live_tri, &c->live_rowoff, &c->totals, &c->vbuf, &c->err,
-                                     &c->stats, &c->cov, &c->plan, &c->galive};
+    const DevBuf *b[kScratchBufs] = {&c->clip,       &c->vdata,      &c->recs,      &c->rows,       &c->chunk_sums,
+                                     &c->live_tri,   &c->live_rowoff, &c->totals,   &c->vbuf,       &c->err,
+                                     &c->stats,      &c->cov,        &c->plan,      &c->galive,     &c->strip_cnt,
+                                     &c->strip_fill, &c->strip_off,  &c->strip_uoff, &c->entries,  &c->unit_strip};
     for (int i = 0; i < kScratchBufs; ++i) out[i] = b[i]->p;
 }
 
@@ -1532,7 +1608,7 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
     const uint64_t *zero_base = (const uint64_t *)(a + off_b);  // every base is 0 for a single scene
     k_prep<<<(unsigned)((tri / kBlock + kBlock - 1) / kBlock), kBlock, 0, st>>>(
         (int *)(a + kNaOffErr), (SceneStats *)(a + kNaOffStats), (uint4 *)(a + kNaOffCov), 1,
-        (uint2 *)(a + kNaOffChunks), tri / kBlock);
+        (uint2 *)(a + kNaOffChunks), tri / kBlock, nullptr, nullptr, 0, (unsigned long long *)(a + kNaOffTotals));
     t_na_nsm = nsm;
     na_dispatch(true, d.shader, dsc, zero_base, vtx / kBlock, a, st);
     k_setup<<<(unsigned)(tri / kBlock), kBlock, 0, st>>>(dsc, nullptr, (const float4 *)(a + kNaOffClip),
@@ -1545,7 +1621,8 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
     k_scan_plan<<<nscan + 1, kBlock, 0, st>>>((const uint32_t *)(a + kNaOffRows), (const uint2 *)(a + kNaOffChunks),
                                               tri, (uint32_t *)(a + kNaOffLiveTri), (uint64_t *)(a + kNaOffLiveOff),
                                               (unsigned long long *)(a + kNaOffTotals), nscan, dsc, 1,
-                                              (const uint4 *)(a + kNaOffCov), ibase, rbase);
+                                              (const uint4 *)(a + kNaOffCov), ibase, rbase, nullptr, 0, nullptr, nullptr,
+                                              nullptr);
     const uint64_t ichunks = (pix + kInitChunk - 1) / kInitChunk + 1;
     k_init<<<chunk_grid(ichunks, nsm), kBlock, 0, st>>>(dsc, ibase, 1, (const uint4 *)(a + kNaOffCov),
                                                          (unsigned long long *)(a + kNaOffVbuf),

@@ -120,7 +120,10 @@ struct SceneDev {
     uint64_t gvtx_base, gvd_base;
     uint32_t geom, gratio, ngin, ntin;
     float gparam;
-    uint32_t pad1;
+    // strip path (strip_h > 0, strip_rows): the target's rows in strips of
+    // strip_h, global strips strip_base .. strip_base + nstrips - 1
+    uint32_t strip_h;
+    uint32_t strip_base, nstrips;
 };
 
 // Per-primitive record written by k_setup (128 bytes, 16-byte aligned).
@@ -173,6 +176,8 @@ constexpr uint32_t kRecAll = 0xFFu;
 struct SceneStats {
     unsigned long long culled;
     unsigned long long candidates;
+    unsigned long long walked;  // fragments the live triangles may make (their screen areas, each at most its bbox)
+    unsigned long long live;    // primitives with at least one row
 };
 
 // ---------------------------------------------------------------------------
@@ -519,6 +524,53 @@ EUC_DEV void setup_line(const SceneDev &s, int si, uint64_t lt, uint64_t t, cons
 constexpr uint32_t kTinyPixels = 4;
 
 // ---------------------------------------------------------------------------
+// The strip path.  A target's rows are cut into strips of strip_h rows that
+// span its whole width, so that no row walk is ever split (a row's weights
+// come from euc's serial additions from its start).  k_strip keeps a strip's
+// visibility keys in shared memory, where a reduction costs little, and
+// walks the strip's (primitive, row) items there.  That pays where many
+// fragments land on each pixel, and each strip entry brings enough of them,
+// so k_bin_count sends a scene's primitives to the strips when its
+// triangles' screen areas add up to kStripOverdraw times its covered
+// rectangle and to kStripTriFrags per triangle or more (or always, when
+// forced), while the entry list has room; kRowsBinned marks them in rows[].  A strip is worked in
+// units of at most kStripUnit entries, one block each: the unit reduces its
+// fragments in shared memory, then merges every key it lowered into the keys
+// k_init seeded with one 64-bit min per pixel.  The other primitives, and the
+// scenes the path does not take (lines, ordered blends, targets too wide for
+// a strip), go through k_raster's item queue after the strips.  Which way a
+// primitive goes changes no result: the keys are order-free reductions.
+// ---------------------------------------------------------------------------
+constexpr int kStripThreads = 512;            // threads of a k_strip block
+constexpr uint32_t kStripMaxRows = 16;        // rows of a strip at most
+constexpr size_t kStripKeyBytes = 96 * 1024;  // a strip's keys in shared memory at most
+constexpr uint32_t kRowsBinned = 0x80000000u; // rows[t]: the primitive went to the strips
+constexpr uint32_t kStripUnit = 1024;         // entries of one strip a k_strip block takes at once at most
+constexpr uint32_t kStripClaim = 64;          // items a k_strip warp claims at a time
+constexpr uint64_t kStripOverdraw = 4;        // fragments per covered pixel that route a scene to the strips ...
+constexpr uint64_t kStripTriFrags = 16;       // ... when its triangles make this many fragments each on average
+constexpr uint64_t kStripMinPixels = 64;      // target pixels per primitive above which a scene stays off them
+constexpr uint32_t kBinHist = 1024;           // strips of a scene the binning kernels count in shared memory
+
+// Keys per row of a strip w pixels wide in shared memory: an odd count, so
+// that the same column of different rows falls in different banks.
+__host__ __device__ inline uint32_t strip_pitch(uint32_t w) { return w | 1u; }
+
+// Rows per strip for a W x H target; 0 when the strip path cannot take it.
+__host__ __device__ inline uint32_t strip_rows(uint32_t W, uint32_t H) {
+    if (W == 0 || H == 0 || H >= (1u << 24) || 8ull * strip_pitch(W) > kStripKeyBytes) return 0;
+    const uint64_t r = kStripKeyBytes / (8ull * strip_pitch(W));
+    return (uint32_t)(r < kStripMaxRows ? r : kStripMaxRows);
+}
+
+// Width bucket of a k_strip entry (its bbox width w): exact below 32, then
+// 16 pixels wide; entries are walked bucket by bucket.
+constexpr uint32_t kWidthBuckets = 64;
+__host__ __device__ inline uint32_t width_bucket(uint32_t w) {
+    return w < 32u ? w : (32u + ((w - 32u) >> 4) < kWidthBuckets - 1 ? 32u + ((w - 32u) >> 4) : kWidthBuckets - 1);
+}
+
+// ---------------------------------------------------------------------------
 // k_setup: triangles.rs:55-199, once per primitive (euc repeats it per band;
 // only the bbox clamp depends on the band and that is applied per row).
 // Block b sets up primitives [b * kBlock, (b + 1) * kBlock), all of scene
@@ -542,6 +594,7 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
     const SceneDev &s = sc[si];
     const uint64_t lt = t - s.tri_base;
     uint32_t nrows = 0, culled = 0;
+    float frag_est = 0.0f;  // the primitive's screen area in pixels, at most its bbox (the strip routing)
     // pixels this primitive may touch: x in [cx0, cx1), y in [cy0, cy1)
     uint32_t cx0 = 0xFFFFFFFFu, cy0 = 0xFFFFFFFFu, cx1 = 0, cy1 = 0;
     if (s.prim != EUC_PRIM_TRIANGLE_LIST) {  // uniform: a block holds one scene
@@ -691,6 +744,8 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
 #pragma unroll
                 for (int k = 0; k < 5; ++k) r.pad[k] = 0;
                 nrows = bx1 > bx0 ? by1 - by0 : 0u;
+                // NDC area |winding| / 2 is (W / 2) x (H / 2) pixels per unit
+                frag_est = fminf(fabsf(winding) * (size_x * size_y * 0.125f), (float)(bx1 - bx0) * (float)(by1 - by0));
                 if (full_rows && (bx1 - bx0) * (by1 - by0) <= kTinyPixels) {
                     // a tiny primitive: walk its few pixels here exactly as
                     // k_raster would (full-bbox rows, triangles.rs:257-301);
@@ -751,13 +806,17 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
         }
     }
     // per-block sums for the scan (zeroed before the launch; each warp adds
-    // its own, no block barrier), and the culled count of this scene
+    // its own, no block barrier), the culled count of this scene, and the
+    // pixels its rows may walk (the strip path's routing)
     const uint32_t live = nrows ? 1u : 0u;
     uint32_t wl = warp_sum(live), wr = warp_sum(nrows), wc = warp_sum(culled);
+    const unsigned long long ww = warp_sum(nrows ? (unsigned long long)frag_est : 0ull);
     if ((threadIdx.x & 31) == 0) {
         if (wl) atomicAdd(&chunk_sums[blockIdx.x].x, wl);
         if (wr) atomicAdd(&chunk_sums[blockIdx.x].y, wr);
         if (wc) atomicAdd(&stats[si].culled, (unsigned long long)wc);
+        if (ww) atomicAdd(&stats[si].walked, ww);
+        if (wl) atomicAdd(&stats[si].live, (unsigned long long)wl);
     }
 }
 
@@ -795,6 +854,7 @@ EUC_DEV void scan_block(const uint32_t *__restrict__ rows, const uint2 *__restri
 #pragma unroll
     for (int k = 0; k < kScanPer; ++k) {
         r[k] = t0 + k < ntri ? rows[t0 + k] : 0u;
+        if (r[k] & kRowsBinned) r[k] = 0;  // walked by k_strip
         my_l += r[k] ? 1 : 0;
         my_r += r[k];
     }
@@ -1227,6 +1287,367 @@ __global__ void __launch_bounds__(kBlock, 4) k_raster(const SceneDev *__restrict
 }
 
 // ---------------------------------------------------------------------------
+// k_bin_count: the strip path's routing and entry counts, after k_setup (a
+// scene's fragment estimate and covered rectangle are complete by then).
+// Blocks stride the setup chunks (each one scene); a chunk of a scene the
+// path does not take costs one check.  A primitive of a scene that the path
+// takes is admitted while the entry list has room: its rows are marked
+// kRowsBinned (the item queue skips it, and its chunk's sums drop it), and
+// each strip it overlaps counts one entry, first in the block's shared
+// memory, then with one global atomic per strip.
+// strip_mode: 0 route by overdraw, 2 every scene the path can take.
+// ---------------------------------------------------------------------------
+EUC_DEV bool strip_routed(const SceneDev &s, const SceneStats &st, const uint4 &cv, uint32_t strip_mode) {
+    return s.strip_h && (strip_mode == 2 || (st.walked >= kStripOverdraw * rect_area(cv) &&
+                                             st.walked >= kStripTriFrags * st.live));
+}
+
+__global__ void __launch_bounds__(kBlock) k_bin_count(const SceneDev *__restrict__ sc,
+                                                      const uint32_t *__restrict__ chunk_scene, uint64_t nchunks,
+                                                      uint32_t *__restrict__ rows, const TriRec *__restrict__ recs,
+                                                      const uint4 *__restrict__ cov,
+                                                      const SceneStats *__restrict__ stats,
+                                                      uint2 *__restrict__ chunk_sums, uint32_t *__restrict__ strip_cnt,
+                                                      unsigned long long *__restrict__ nentries, uint64_t entry_cap,
+                                                      uint32_t strip_mode) {
+    __shared__ uint32_t s_hist[kBinHist];
+    const int lane = threadIdx.x & 31;
+    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {  // uniform over the block
+        const int si = chunk_scene ? (int)chunk_scene[c] : 0;
+        const SceneDev &s = sc[si];
+        if (!strip_routed(s, stats[si], cov[si], strip_mode)) continue;
+        const uint64_t t = c * kBlock + threadIdx.x;
+        const bool local = s.nstrips <= kBinHist;
+        __syncthreads();  // the previous chunk's flush is done with the histogram
+        for (uint32_t q = threadIdx.x; local && q < s.nstrips; q += kBlock) s_hist[q] = 0;
+        const uint32_t nr = rows[t];
+        uint32_t q0 = 0, nst = 0;
+        if (nr) {
+            const uint4 w3 = __ldg(reinterpret_cast<const uint4 *>(recs + t) + 3);  // bx0, bx1, by0, by1
+            q0 = w3.z / s.strip_h;
+            nst = (w3.w - 1) / s.strip_h - q0 + 1;
+        }
+        // admission, in warp order while the entry list has room
+        const uint32_t inc = warp_incl_scan(nst), tot = __shfl_sync(0xFFFFFFFFu, inc, 31);
+        unsigned long long at = 0;
+        if (lane == 31 && tot) at = atomicAdd(nentries, (unsigned long long)tot);
+        at = __shfl_sync(0xFFFFFFFFu, at, 31);
+        const bool binned = nst && at + inc <= entry_cap;
+        __syncthreads();  // the histogram is clear
+        if (binned) {
+            rows[t] = nr | kRowsBinned;
+            for (uint32_t k = 0; k < nst; ++k) {
+                if (local) atomicAdd(s_hist + q0 + k, 1u);
+                else atomicAdd(strip_cnt + s.strip_base + q0 + k, 1u);
+            }
+        }
+        const uint32_t bl = warp_sum(binned ? 1u : 0u), br = warp_sum(binned ? nr : 0u);
+        if (lane == 0 && bl) {
+            atomicSub(&chunk_sums[c].x, bl);
+            atomicSub(&chunk_sums[c].y, br);
+        }
+        __syncthreads();
+        for (uint32_t q = threadIdx.x; local && q < s.nstrips; q += kBlock)
+            if (s_hist[q]) atomicAdd(strip_cnt + s.strip_base + q, s_hist[q]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_bin: the strip lists.  Every admitted primitive (kRowsBinned) adds one
+// entry {primitive, first row << 16 | end row} (rows relative to the strip)
+// to each strip it overlaps; the order within a list does not matter.
+// Blocks stride the setup chunks (each one scene): a chunk counts its entries
+// per strip in shared memory, reserves each strip's range with one global
+// atomic, then writes the entries.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_bin(const SceneDev *__restrict__ sc, const uint32_t *__restrict__ chunk_scene,
+                                                uint64_t nchunks, const uint32_t *__restrict__ rows,
+                                                const TriRec *__restrict__ recs, const uint4 *__restrict__ cov,
+                                                const SceneStats *__restrict__ stats,
+                                                const uint32_t *__restrict__ strip_off, uint32_t *__restrict__ strip_fill,
+                                                uint2 *__restrict__ entries, uint32_t strip_mode) {
+    __shared__ uint32_t s_cnt[kBinHist], s_base[kBinHist];
+    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {  // uniform over the block
+        const int si = chunk_scene ? (int)chunk_scene[c] : 0;
+        const SceneDev &s = sc[si];
+        if (!strip_routed(s, stats[si], cov[si], strip_mode)) continue;
+        const uint64_t t = c * kBlock + threadIdx.x;
+        const bool local = s.nstrips <= kBinHist;
+        __syncthreads();  // the previous chunk is done with the counts
+        for (uint32_t q = threadIdx.x; local && q < s.nstrips; q += kBlock) s_cnt[q] = 0;
+        const uint32_t h = s.strip_h;
+        uint32_t by0 = 0, by1 = 0, q0 = 0, nst = 0;
+        if (rows[t] & kRowsBinned) {
+            const uint4 w3 = __ldg(reinterpret_cast<const uint4 *>(recs + t) + 3);  // bx0, bx1, by0, by1
+            by0 = w3.z;
+            by1 = w3.w;
+            q0 = by0 / h;
+            nst = (by1 - 1) / h - q0 + 1;
+        }
+        __syncthreads();
+        if (local) {
+            for (uint32_t k = 0; k < nst; ++k) atomicAdd(s_cnt + q0 + k, 1u);
+            __syncthreads();
+            for (uint32_t q = threadIdx.x; q < s.nstrips; q += kBlock) {
+                const uint32_t n = s_cnt[q];
+                if (n) s_base[q] = strip_off[s.strip_base + q] + atomicAdd(strip_fill + s.strip_base + q, n);
+                s_cnt[q] = 0;
+            }
+            __syncthreads();
+        }
+        for (uint32_t k = 0; k < nst; ++k) {
+            const uint32_t q = q0 + k, g = s.strip_base + q, s0 = q * h;
+            const uint32_t pos = local ? s_base[q] + atomicAdd(s_cnt + q, 1u) : strip_off[g] + atomicAdd(strip_fill + g, 1u);
+            const uint32_t ya = max(by0, s0) - s0, yb = min(by1, s0 + h) - s0;
+            entries[pos] = make_uint2((uint32_t)t, (ya << 16) | yb);
+        }
+    }
+}
+
+// Shared-memory 64-bit min reduction (no value returned).
+EUC_DEV void smem_min_u64(uint32_t saddr, unsigned long long v) {
+    asm volatile("red.shared.min.u64 [%0], %1;" ::"r"(saddr), "l"(v) : "memory");
+}
+
+// walk_row for a strip: the same serial walk (triangles.rs:257-301), with
+// the keys in shared memory; `srow` is the shared address of the row's key
+// for x = 0 (8 bytes per pixel).  KEY_MIN or KEY_LAST scenes.
+EUC_DEV void strip_walk_row(const SceneDev &s, const TriRec &r, uint32_t t, uint32_t y, uint32_t xs, uint32_t xe,
+                            uint32_t srow, uint32_t &cnt) {
+    const float yf = (float)y;
+    const float xsf = (float)xs;
+    float w0 = (r.o[0] + r.dy[0] * yf) + r.dx[0] * xsf;
+    float w1 = (r.o[1] + r.dy[1] * yf) + r.dx[1] * xsf;
+    float w2 = (r.o[2] + r.dy[2] * yf) + r.dx[2] * xsf;
+    const float d0 = r.dx[0], d1 = r.dx[1], d2 = r.dx[2];
+    const float z0 = r.zc[0], z1 = r.zc[1], z2 = r.zc[2];
+    const bool noclip = r.flags & 1u;
+    const float zmin = s.zmin, zmax = s.zmax;
+    if (s.keytype == KEY_MIN) {
+        const uint32_t flip = s.depth_test == EUC_TEST_GREATER ? 0xFFFFFFFFu : 0u;
+        const uint32_t tmin = (t + 1u) << 1;
+#pragma unroll 4
+        for (uint32_t x = xs; x < xe; ++x) {
+            const float wu2 = (w2 - w0) - w1;
+            if (w0 >= 0.0f && w1 >= 0.0f && wu2 >= 0.0f) {
+                const float z = (z0 * w0 + z1 * w1) + z2 * wu2;
+                if (noclip || (zmin <= z && z <= zmax)) {
+                    ++cnt;
+                    if (z == z) {  // a NaN depth fails every test (partial_cmp is None)
+                        const uint32_t b = __float_as_uint(z + 0.0f);  // -0 and +0 compare equal
+                        const uint32_t o = (b ^ ((uint32_t)((int32_t)b >> 31) | 0x80000000u)) ^ flip;
+                        const uint32_t neg0 = __float_as_uint(z) == 0x80000000u ? 1u : 0u;
+                        smem_min_u64(srow + 8u * x, ((unsigned long long)o << 32) | (tmin | neg0));
+                    }
+                }
+            }
+            w0 = w0 + d0;
+            w1 = w1 + d1;
+            w2 = w2 + d2;
+        }
+        return;
+    }
+    // KEY_LAST: every fragment against the unchanged initial depth
+    const float *row_depth = s.depth ? reinterpret_cast<const float *>(s.depth + (uint64_t)y * s.dpitch) : nullptr;
+    const unsigned long long tlast = (unsigned long long)(~t) << 32;
+    for (uint32_t x = xs; x < xe; ++x) {
+        const float wu2 = (w2 - w0) - w1;
+        if (w0 >= 0.0f && w1 >= 0.0f && wu2 >= 0.0f) {
+            const float z = (z0 * w0 + z1 * w1) + z2 * wu2;
+            if (noclip || (zmin <= z && z <= zmax)) {
+                ++cnt;
+                bool pass = true;
+                if (s.depth_test != EUC_TEST_NONE) {
+                    const float old = row_depth[x];
+                    if (s.depth_test == EUC_TEST_LESS) pass = z < old;
+                    else if (s.depth_test == EUC_TEST_EQUAL) pass = z == old;
+                    else pass = z > old;
+                }
+                if (pass) smem_min_u64(srow + 8u * x, tlast | __float_as_uint(z));
+            }
+        }
+        w0 = w0 + d0;
+        w1 = w1 + d1;
+        w2 = w2 + d2;
+    }
+}
+
+// Block-wide exclusive scan over kStripThreads threads (k_strip).
+EUC_DEV uint32_t strip_block_scan(uint32_t v, uint32_t *smem /* >= kStripThreads/32 + 1 */, uint32_t *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t inc = warp_incl_scan(v);
+    if (lane == 31) smem[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t x = lane < kStripThreads / 32 ? smem[lane] : 0u;
+        const uint32_t xi = warp_incl_scan(x);
+        if (lane < kStripThreads / 32) smem[lane] = xi - x;
+        if (lane == kStripThreads / 32 - 1) smem[kStripThreads / 32] = xi;
+    }
+    __syncthreads();
+    const uint32_t r = smem[warp] + inc - v;
+    *total = smem[kStripThreads / 32];
+    __syncthreads();
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// k_strip: one unit (up to kStripUnit entries of one strip) at a time per
+// block, claimed from a work counter (totals[7]).  sbase: the first strip of
+// each scene (nsc + 1 entries).  The unit's keys over the strip's rows inside
+// the scene's covered rectangle start at ~0 in shared memory; the warps
+// claim runs of kStripClaim items of its entries from a shared counter and
+// walk them with shared-memory reductions; every key the unit lowered is
+// then merged into vbuf (which k_init seeded) with one 64-bit min.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kStripThreads, 2) k_strip(const SceneDev *__restrict__ sc,
+                                                            const uint64_t *__restrict__ sbase, int nsc,
+                                                            const uint4 *__restrict__ cov,
+                                                            const uint32_t *__restrict__ strip_off,
+                                                            const uint32_t *__restrict__ strip_uoff,
+                                                            const uint32_t *__restrict__ unit_strip,
+                                                            const uint2 *__restrict__ entries,
+                                                            const TriRec *__restrict__ recs,
+                                                            const int *__restrict__ err,
+                                                            unsigned long long *__restrict__ vbuf,
+                                                            SceneStats *__restrict__ stats,
+                                                            unsigned long long *__restrict__ totals) {
+    extern __shared__ unsigned long long s_keys[];  // rows [r0, r1) x columns [cx0, cx1) of the strip
+    __shared__ uint32_t s_pref[kStripUnit];         // first item of each entry of the unit (in width order)
+    __shared__ uint32_t s_t[kStripUnit];            // its primitive
+    __shared__ uint8_t s_ya[kStripUnit];            // its first row within the strip
+    __shared__ uint8_t s_nr[kStripUnit];            // its rows within the strip
+    __shared__ uint32_t s_bkt[kWidthBuckets];       // entries per width bucket, then the bucket's first position
+    __shared__ uint32_t s_scan[kStripThreads / 32 + 1];
+    __shared__ uint32_t s_u, s_next;
+    static_assert(2 * kStripThreads == kStripUnit && kStripMaxRows <= 255, "two entries per thread, rows in 8 bits");
+    static_assert(offsetof(TriRec, bx0) == 48, "k_strip reads the bbox width from 8-byte word 6 of a record");
+    const int tid = threadIdx.x, lane = tid & 31;
+    const uint32_t nstrips = (uint32_t)sbase[nsc];
+    const uint32_t nunits = strip_uoff[nstrips];
+    const uint32_t keys_saddr = (uint32_t)__cvta_generic_to_shared(s_keys);
+    for (;;) {
+        if (tid == 0) {
+            s_u = (uint32_t)atomicAdd(totals + 7, 1ull);
+            s_next = 0;
+        }
+        __syncthreads();
+        const uint32_t u = s_u;
+        if (u >= nunits) break;
+        const uint32_t g = unit_strip[u];
+        const int si = find_scene(sbase, nsc, g);
+        const SceneDev &s = sc[si];
+        const uint4 cv = cov[si];
+        const uint32_t s0 = (g - s.strip_base) * s.strip_h;
+        // every entry's rows lie in the strip and in the covered rectangle
+        const uint32_t r0 = max(s0, cv.y), r1 = min(min(s0 + s.strip_h, s.H), ~cv.w);
+        const uint32_t cx0 = cv.x, cx1 = ~cv.z;
+        const bool empty = r0 >= r1 || cx0 >= cx1;  // never for a strip with entries
+        const uint32_t wc = empty ? 0u : cx1 - cx0, area = empty ? 0u : (r1 - r0) * strip_pitch(wc);
+        const uint32_t pitch = strip_pitch(wc);
+        const uint32_t e_begin = strip_off[g] + (u - strip_uoff[g]) * kStripUnit;
+        const int nload = (int)(min(e_begin + kStripUnit, strip_off[g + 1]) - e_begin);
+        // the unit's entries, two per thread, ordered by bbox width (a
+        // counting sort over kWidthBuckets), so that the rows a warp walks
+        // together have about the same length
+        if (tid < (int)kWidthBuckets) s_bkt[tid] = 0;
+        uint2 ev[2];
+        uint32_t bk[2], rk[2];
+        __syncthreads();
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int k = 2 * tid + h;
+            ev[h] = make_uint2(0u, 0u);
+            bk[h] = 0xFFFFFFFFu;
+            if (k < nload) {
+                ev[h] = entries[e_begin + k];
+                const uint2 bx = __ldg(reinterpret_cast<const uint2 *>(recs + ev[h].x) + 6);  // bx0, bx1
+                bk[h] = width_bucket(bx.y - bx.x);
+            }
+            const uint32_t m = __match_any_sync(0xFFFFFFFFu, bk[h]);
+            const int leader = __ffs(m) - 1;
+            uint32_t base = 0;
+            if (bk[h] != 0xFFFFFFFFu && lane == leader) base = atomicAdd(s_bkt + bk[h], (uint32_t)__popc(m));
+            rk[h] = __shfl_sync(0xFFFFFFFFu, base, leader) + __popc(m & ((1u << lane) - 1u));
+        }
+        __syncthreads();
+        if (tid < 32) {  // bucket sizes -> first positions
+            static_assert(kWidthBuckets == 64, "two buckets per lane");
+            const uint32_t c0 = s_bkt[2 * lane], c1 = s_bkt[2 * lane + 1];
+            const uint32_t inc = warp_incl_scan(c0 + c1);
+            s_bkt[2 * lane] = inc - c0 - c1;
+            s_bkt[2 * lane + 1] = inc - c1;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (bk[h] == 0xFFFFFFFFu) continue;
+            const uint32_t d = s_bkt[bk[h]] + rk[h];
+            s_t[d] = ev[h].x;
+            s_ya[d] = (uint8_t)(ev[h].y >> 16);
+            s_nr[d] = (uint8_t)((ev[h].y & 0xFFFFu) - (ev[h].y >> 16));
+        }
+        __syncthreads();
+        const uint32_t n0 = 2 * tid < nload ? s_nr[2 * tid] : 0u, n1 = 2 * tid + 1 < nload ? s_nr[2 * tid + 1] : 0u;
+        uint32_t total;
+        const uint32_t pre = strip_block_scan(n0 + n1, s_scan, &total);
+        s_pref[2 * tid] = pre;
+        s_pref[2 * tid + 1] = pre + n0;
+        for (uint32_t i = tid; i < area; i += kStripThreads) s_keys[i] = ~0ull;
+        __syncthreads();
+        uint32_t cnt = 0;
+        if (!err[si] && !empty) {  // a scene with a bad index draws nothing
+            for (;;) {
+                uint32_t i0 = 0;
+                if (lane == 0) i0 = atomicAdd(&s_next, kStripClaim);
+                i0 = __shfl_sync(0xFFFFFFFFu, i0, 0);
+                if (i0 >= total) break;
+                int lo = 0, hi = nload;  // the entry of item i0: largest a with s_pref[a] <= i0
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (s_pref[mid] <= i0) lo = mid; else hi = mid;
+                }
+                int a0 = lo;
+                const uint32_t iend = min(total, i0 + kStripClaim);
+                // 32 consecutive items at a time: their entries are a run from
+                // a0 (every entry has at least one row)
+                for (uint32_t j0 = i0; j0 < iend; j0 += 32) {
+                    const int c = a0 + 1 + lane;
+                    uint32_t bit = 0;
+                    if (lane < 31 && c < nload) {
+                        const uint32_t o = s_pref[c];
+                        if (o > j0 && o < j0 + 32) bit = 1u << (o - j0);
+                    }
+                    const uint32_t starts = __reduce_or_sync(0xFFFFFFFFu, bit);
+                    const int a = a0 + __popc(starts & ((2u << lane) - 1u));
+                    const int alast = a0 + __popc(starts);
+                    a0 = (alast + 1 < nload && s_pref[alast + 1] == j0 + 32) ? alast + 1 : alast;
+                    const uint32_t i = j0 + lane;
+                    if (i >= iend) continue;
+                    const uint32_t t = s_t[a];
+                    const uint32_t y = s0 + s_ya[a] + (i - s_pref[a]);
+                    const TriRec r = load_rec(recs + t, kRecRaster);
+                    uint32_t xs, xe;
+                    if (!row_span(s, r, y, xs, xe)) continue;
+                    strip_walk_row(s, r, t, y, xs, xe, keys_saddr + 8u * ((y - r0) * pitch) - 8u * cx0, cnt);
+                }
+            }
+        }
+        __syncthreads();
+        // merge the keys this unit lowered, and its candidates
+        unsigned long long *dst = vbuf + s.pix_base;
+        for (uint32_t i = tid; i < area; i += kStripThreads) {
+            const unsigned long long k = s_keys[i];
+            const uint32_t ry = i / pitch, rx = i - ry * pitch;
+            if (k != ~0ull && rx < wc) atomicMin(dst + (uint64_t)(r0 + ry) * s.W + cx0 + rx, k);
+        }
+        const uint32_t wsum = warp_sum(cnt);
+        if (lane == 0 && wsum) atomicAdd(&stats[si].candidates, (unsigned long long)wsum);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // k_resolve<F>: shade the winner of every pixel and write colour / depth.
 // ---------------------------------------------------------------------------
 template <class F>
@@ -1391,9 +1812,61 @@ EUC_DEV void plan_chunks(const SceneDev *__restrict__ sc, int nsc, const uint4 *
     }
 }
 
-// The scan of the setup's row counts (blocks 0 .. nscan - 1, scan_block) and
-// the chunk plan of init / resolve (block nscan, plan_chunks): independent
-// work after k_setup, in one launch.
+// Exclusive scans of the strips' entry counts into their list offsets, and
+// of their units (ceil(count / kStripUnit)) into unit offsets (nstrips + 1
+// entries each), and the strip of every unit.  Block b covers strips
+// [b*kScanBlock, (b+1)*kScanBlock) and sums the strips before them itself.
+EUC_DEV void strip_scan_block(uint32_t b, const uint32_t *__restrict__ cnt, uint32_t nstrips,
+                              uint32_t *__restrict__ off, uint32_t *__restrict__ uoff,
+                              uint32_t *__restrict__ unit_strip) {
+    __shared__ uint32_t s_a[kBlock / 32 + 1];
+    __shared__ uint32_t s_pre[2];
+    const uint64_t g0 = (uint64_t)b * kScanBlock;
+    uint32_t pre = 0, preu = 0;
+    for (uint64_t j = threadIdx.x; j < g0; j += kBlock) {
+        pre += cnt[j];
+        preu += (cnt[j] + kStripUnit - 1) / kStripUnit;
+    }
+    uint32_t tp, tu;
+    block_excl_scan<uint32_t>(pre, s_a, &tp);
+    block_excl_scan<uint32_t>(preu, s_a, &tu);
+    if (threadIdx.x == 0) {
+        s_pre[0] = tp;
+        s_pre[1] = tu;
+    }
+    __syncthreads();
+    const uint64_t q0 = g0 + (uint64_t)threadIdx.x * kScanPer;
+    uint32_t c[kScanPer], mine = 0, mineu = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {
+        c[k] = q0 + k < nstrips ? cnt[q0 + k] : 0u;
+        mine += c[k];
+        mineu += (c[k] + kStripUnit - 1) / kStripUnit;
+    }
+    uint32_t bt, btu;
+    uint32_t o = s_pre[0] + block_excl_scan<uint32_t>(mine, s_a, &bt);
+    uint32_t ou = s_pre[1] + block_excl_scan<uint32_t>(mineu, s_a, &btu);
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {
+        const uint32_t nu = (c[k] + kStripUnit - 1) / kStripUnit;
+        if (q0 + k < nstrips) {
+            off[q0 + k] = o;
+            uoff[q0 + k] = ou;
+            for (uint32_t u = 0; u < nu; ++u) unit_strip[ou + u] = (uint32_t)(q0 + k);
+        }
+        o += c[k];
+        ou += nu;
+    }
+    if (g0 + kScanBlock >= nstrips && threadIdx.x == kBlock - 1) {
+        off[nstrips] = s_pre[0] + bt;
+        uoff[nstrips] = s_pre[1] + btu;
+    }
+}
+
+// The scan of the setup's row counts (blocks 0 .. nscan - 1, scan_block), the
+// chunk plan of init / resolve (block nscan, plan_chunks) and the scans of
+// the strips (the blocks after, strip_scan_block): independent work after
+// k_setup, in one launch.
 __global__ void __launch_bounds__(kBlock) k_scan_plan(const uint32_t *__restrict__ rows,
                                                       const uint2 *__restrict__ chunk_sums, uint64_t ntri,
                                                       uint32_t *__restrict__ live_tri,
@@ -1401,16 +1874,24 @@ __global__ void __launch_bounds__(kBlock) k_scan_plan(const uint32_t *__restrict
                                                       unsigned long long *__restrict__ totals, uint32_t nscan,
                                                       const SceneDev *__restrict__ sc, int nsc,
                                                       const uint4 *__restrict__ cov, uint64_t *__restrict__ ibase,
-                                                      uint64_t *__restrict__ rbase) {
+                                                      uint64_t *__restrict__ rbase, const uint32_t *__restrict__ strip_cnt,
+                                                      uint32_t nstrips, uint32_t *__restrict__ strip_off,
+                                                      uint32_t *__restrict__ strip_uoff, uint32_t *__restrict__ unit_strip) {
     if (blockIdx.x == nscan) plan_chunks(sc, nsc, cov, ibase, rbase);
+    else if (blockIdx.x > nscan)
+        strip_scan_block(blockIdx.x - nscan - 1, strip_cnt, nstrips, strip_off, strip_uoff, unit_strip);
     else scan_block(rows, chunk_sums, ntri, live_tri, live_rowoff, totals, nscan);
 }
 
 // Per batch, before k_setup: no errors, zero statistics, empty covered
-// rectangles, zero setup-chunk sums.
+// rectangles, zero setup-chunk sums, zero strip counts and fill cursors, and
+// the strip path's counters (totals[6]: entries taken, totals[7]: k_strip's
+// work counter).
 __global__ void __launch_bounds__(kBlock) k_prep(int *__restrict__ err, SceneStats *__restrict__ stats,
                                                  uint4 *__restrict__ cov, int nsc, uint2 *__restrict__ chunk_sums,
-                                                 uint64_t nchunks) {
+                                                 uint64_t nchunks, uint32_t *__restrict__ strip_cnt,
+                                                 uint32_t *__restrict__ strip_fill, uint32_t nstrips,
+                                                 unsigned long long *__restrict__ totals) {
     const uint64_t i = (uint64_t)blockIdx.x * kBlock + threadIdx.x;
     if (i < (uint64_t)nsc) {
         err[i] = 0;
@@ -1418,6 +1899,11 @@ __global__ void __launch_bounds__(kBlock) k_prep(int *__restrict__ err, SceneSta
         cov[i] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
     }
     if (i < nchunks) chunk_sums[i] = make_uint2(0u, 0u);
+    if (i < nstrips) {
+        strip_cnt[i] = 0;
+        strip_fill[i] = 0;
+    }
+    if (i < 2) totals[6 + i] = 0;
 }
 
 template <class F>

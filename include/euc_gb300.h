@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define EUC_ABI_VERSION 1
+#define EUC_ABI_VERSION 2
 
 /* ------------------------------------------------------------------------ */
 /* Status codes.  euc reports failures by panicking; each panic site maps to
@@ -303,6 +303,7 @@ typedef struct euc_tuning {
     uint32_t chunk_blocks_per_sm;  /* init/resolve grid cap per SM (16)                              */
     uint32_t raster_probe;         /* 1: read a key before its atomicMin, 2: atomics only (default)  */
     uint32_t host_copy;            /* host-buffer renders: EUC_HOST_COPY_* (AUTO)                    */
+    uint32_t strip_path;           /* shared-memory strips: 0 for overdrawn scenes, 1 off, 2 always  */
 } euc_tuning;
 
 /* How euc_render_host / euc_render_host_batch reach host buffers.  DIRECT

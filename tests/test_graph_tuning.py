@@ -141,6 +141,9 @@ SHAPES = [
     dict(chunk_group=1024, chunk_blocks_per_sm=64, raster_warp_rows=224, raster_blocks_per_sm=2),
     dict(raster_probe=2),
     dict(raster_probe=1, raster_warp_rows=64),
+    dict(strip_path=1),
+    dict(strip_path=2),
+    dict(strip_path=2, raster_warp_rows=64, chunk_group=1),
 ]
 
 
@@ -170,7 +173,8 @@ def test_launch_shapes_do_not_change_results(which):
 
 @pytest.mark.parametrize("bad", [dict(raster_warp_rows=48), dict(raster_warp_rows=288),
                                  dict(raster_blocks_per_sm=65), dict(chunk_group=1025),
-                                 dict(chunk_blocks_per_sm=100), dict(raster_probe=3)])
+                                 dict(chunk_blocks_per_sm=100), dict(raster_probe=3),
+                                 dict(strip_path=3)])
 def test_invalid_launch_shapes_are_refused(bad):
     ctx = capi.Context(0)
     try:
