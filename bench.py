@@ -11,16 +11,28 @@ in HBM for `value`.
 
 Printed as one JSON line (rank 0):
   value        batched scenes/s through euc_render_batch (whole job)
-  per_scene    scenes/s for the same scenes through euc_render one at a time
+  per_scene    scenes/s for the same scenes through euc_render one scene pass
+               at a time, with the call arguments built once
   e2e          scenes/s through the blocking host-buffer batch call
                euc_render_host_batch (host->device copies of inputs and targets,
                device->host copy of the targets, all inside the timed region);
                per_scene_value: the same through euc_render_host per scene
   mfrag_per_s  candidate fragments (inside + z-clip, exact counts) per second
   roofline     algorithmic bytes per batch / the dominant stage's CUDA-event
-               time per batch, against the measured HBM copy bandwidth
+               time per batch, against the measured HBM copy bandwidth; the
+               stage's kernels' DRAM bytes (ncu, profiles/traffic.json) over
+               the same time; and `issue`: candidate fragments per second of
+               the raster stage against every issue slot running full warps of
+               the fewest instructions a candidate needs
+  pipeline_roofline  the whole step's algorithmic bytes against the same peak
   cpu_baseline the CPU oracle (a port of euc's render_par: row bands over all
                host threads) on a bounded sample of the same scenes
+  other_configs  measured after the headline in the same process (unless
+               --no-extras): the 640x480 sphere stream (1024 frames per step),
+               the 1080p 200k-triangle soup, the two-pass torus knot (4 frames
+               per step), each batched and per scene with rates, stage times
+               and rooflines, and a serving sweep at 2k, 10k and 50k
+               requests/s (--serve-short-seconds each), with their own clocks
 
 With --impl reference the CPU oracle is timed alone on the same workload (the
 reference's CPU path; euc itself is Rust and cannot be built here).
@@ -82,6 +94,10 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="serve: length of each rate's run")
     ap.add_argument("--max-batch", type=int, default=256, help="serve: requests per batch at most")
     ap.add_argument("--slots", type=int, default=3, help="serve: batches in flight at once")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="batch: skip the other configurations (sphere, soup, knot, serving) after the headline")
+    ap.add_argument("--serve-short-seconds", type=float, default=2.0,
+                    help="the serving sweep's length per rate when it runs after the headline")
     args = ap.parse_args()
     if args.workload != "batch":
         args.scenes = args.frames or WORKLOADS[args.workload][1]
@@ -361,83 +377,81 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
-def load_traffic():
-    path = os.path.join(ROOT, "profiles", "traffic.json")
+def load_profile_json(name):
+    """A summary committed under profiles/ (ncu figures), or None."""
     try:
-        with open(path) as fh:
+        with open(os.path.join(ROOT, "profiles", name)) as fh:
             return json.load(fh)
     except (OSError, ValueError):
         return None
 
 
-def run_gpu(args):
+# The kernels each profiled stage holds (CUDA-event stage times).
+STAGE_KERNELS = {"vertex": ["k_vertex"], "setup": ["k_setup", "k_bin_count"], "scan": ["k_scan_plan"],
+                 "init": ["k_init"], "raster": ["k_bin", "k_strip", "k_raster"], "resolve": ["k_resolve"]}
+
+# The fewest thread instructions a candidate fragment needs in euc's walk
+# (triangles.rs:257-301): three additions that advance the weights, two for
+# the third weight, three compares, the z dot product (three multiplies, two
+# additions), the key (five integer operations) and its reduction.
+MIN_INST_PER_CANDIDATE = 19
+
+
+def prebuilt_render_calls(ctx, batch, sp):
+    """The euc_render argument tuples of every scene pass of `batch`, built
+    once, as a caller that holds its pipeline, uniforms and buffers calls
+    it: pass k of every frame after pass k - 1 of every frame."""
+    import ctypes as C
+    calls = []
+    for arr in batch.scene_arrays():
+        for sc in arr:
+            calls.append((ctx.handle, C.byref(sc.desc), sc.uniforms, sc.uniforms_size, C.byref(sc.layout),
+                          sc.vertices, sc.nverts, sc.indices, sc.nindices, C.byref(sc.pixel), C.byref(sc.depth), sp))
+    return calls
+
+
+def measure(ctx, specs, dev, stream, steps, warmup, tune, graph_ok=True, world=1, tune_reps=9, per_scene_reps=2):
+    """One workload on the GPU: the batched form (plain calls with per-stage
+    CUDA events, and the recorded graph), the candidate count of one step,
+    and the plain per-scene path (euc_render per scene pass, arguments built
+    once).  Times are device times of `steps` steps, max over ranks."""
     import torch
     import torch.distributed as dist
-    from euc_gb300 import capi, replicas, frames as fr
+    from euc_gb300 import abi, capi, replicas, frames as fr
 
-    world, rank, local = dist_env()
-    if world > 1:
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    torch.cuda.set_device(local)
-    dev = "cuda:%d" % local
-    specs = make_frames(args, rank)
-    ctx = capi.Context(local)
     batch = fr.DeviceBatch(specs, dev)
-    stream = torch.cuda.current_stream()
 
     def step():
         fr.render_batch(ctx, batch, stream, clear=True)
 
     tuning, tune_info = None, None
-    if not args.no_tune:
+    if tune:
         from euc_gb300 import autotune
-        tuning, tune_info = autotune.tune(ctx, batch, stream, reps=9)
-    # the recorded form of the same batch (scenes on the ordered path cannot be recorded)
+        tuning, tune_info = autotune.tune(ctx, batch, stream, reps=tune_reps)
     graph = None
-    if not args.no_graph and not any(s.desc.blend == 1 or s.desc.flags & 2 for arr in batch.scene_arrays()
-                                     for s in arr):
+    if graph_ok and not any(s.desc.blend == 1 or s.desc.flags & 2 for arr in batch.scene_arrays() for s in arr):
         graph = fr.BatchGraph(ctx, batch)
-
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(max(warmup, 3)):
         step()
         if graph:
             graph.launch(stream)
     capi.check(ctx.sync(fr._stream_ptr(stream)), "warm-up")
-    # candidate fragments of one step, pass by pass (stats cover one batch call)
-    cand_per_step = 0
+    # candidate fragments of one step, pass by pass (statistics cover one batch call)
+    cand = 0
     batch.clear()
-    npass = max(len(f.frame.passes) for f in batch.frames)
-    for k in range(npass):
-        scenes_k, keep = [], []
-        for df in batch.frames:
-            if k < len(df.frame.passes):
-                s, kp = df.scene(k)
-                scenes_k.append(s)
-                keep.append(kp)
-        capi.check(ctx.render_batch(scenes_k, fr._stream_ptr(stream)), "render_batch")
-        cand_per_step += ctx.stats(fr._stream_ptr(stream)).candidates
-    ctx.profile()  # reset counters
+    sp = fr._stream_ptr(stream)
+    for arr in batch.scene_arrays():
+        capi.check(ctx.render_scene_array(arr, sp), "render_batch")
+        cand += ctx.stats(sp).candidates
+    ctx.profile()  # reset the counters
 
-    bus = None
-    try:
-        bus = torch.cuda.get_device_properties(local).pci_bus_id
-    except AttributeError:
-        pass
-    clocks = ClockSampler(bus)
-    ctx.set_profiling(True)
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    time.sleep(0.3)
-
-    def timed(fn):
+    def timed(fn, n):
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(n):
             fn()
         e1.record(stream)
         torch.cuda.synchronize()
@@ -446,130 +460,94 @@ def run_gpu(args):
             dist.barrier()
         return t
 
-    # plain calls with per-stage CUDA events (the stage times of the roofline)
-    ms_plain = timed(step)
+    ctx.set_profiling(True)
+    ms_plain = timed(step, steps)
     ctx.set_profiling(False)
     stage_ms, launches = ctx.profile()
-    ms_graph = None
+    ms_graph, graph_launches = None, None
     if graph:
-        ms_graph = timed(lambda: graph.launch(stream))
+        ms_graph = timed(lambda: graph.launch(stream), steps)
         _, graph_launches = ctx.profile()
-    clk = clocks.stop()
-    ms = min(ms_plain, ms_graph) if ms_graph else ms_plain
     form = "graph" if ms_graph and ms_graph <= ms_plain else "plain"
-    if form == "graph":
-        launches = graph_launches
-    ms_step = ms / args.steps
-    value = world * args.scenes / (ms_step / 1e3)
-
-    # per-scene plain path on the same scenes (euc_render, one call per scene)
-    def per_scene_pass():
-        batch.clear()
-        for df in batch.frames:
-            fr.render_frame(ctx, df, stream, clear=False)
-    per_scene = e2e = e2e_per_scene = None
-    if not args.only_batched:
-        # the per-scene paths run with the default launch shape (the tuned one
-        # is chosen for the batch)
+    ms = ms_graph if form == "graph" else ms_plain
+    # the plain per-scene path with the default launch shape
+    per_scene = None
+    if per_scene_reps:
         tuned = ctx.get_tuning()
         ctx.set_tuning(None)
-        per_scene_pass()
-        torch.cuda.synchronize()
-        reps = max(2, args.steps // 4)
-        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        p0.record(stream)
-        for _ in range(reps):
-            per_scene_pass()
-        p1.record(stream)
-        torch.cuda.synchronize()
-        per_scene = args.scenes / (p0.elapsed_time(p1) / reps / 1e3)
-        e2e_per_scene = run_e2e(ctx, specs, reps=1)
-        ctx.set_tuning(tuned)
-        e2e = run_e2e_batch(ctx, specs, reps=max(2, min(args.steps, 5)))
-    h2d, d2h = host_bytes(specs)
-    host_copy = ("in place: kernels read vertices and indices and update targets in host memory over "
-                 "NVLink-C2C; one kernel gathers the textures") if ctx.host_copy_direct() else \
-        "staged through page-locked memory by host threads, one copy each way"
+        calls = prebuilt_render_calls(ctx, batch, sp)
+        render = capi.lib().euc_render
 
-    alg_bytes = sum(f.algorithmic_bytes() for f in specs)
-    # each step also clears every target first, as euc's own bench loop does
-    # (benches/teapot.rs:182-184): one more write of each target
-    clear_bytes = sum(t.width * t.height * t.bpp for f in specs for t in f.targets)
-    dom = max(stage_ms, key=lambda k: stage_ms[k])
-    dom_ms = stage_ms[dom] / args.steps
-    peak, peak_kind = load_peaks()
-    achieved = alg_bytes / (dom_ms / 1e3) / 1e9
-    traffic = load_traffic()
-    cpu = None
-    if rank == 0 and not args.no_baseline and not args.only_batched:
-        n, t, threads = cpu_sample(specs, args.cpu_seconds)
-        cpu = {"value": n / t, "unit": WORKLOADS[args.workload][2], "cores": threads, "kind": "port",
-               "sample": "%d scenes (rotating through the %d of one step) in %.1f s (oracle render_par, %d threads)"
-                         % (n, len(specs), t, threads)}
-    if rank == 0:
-        desc, _, unit = WORKLOADS[args.workload]
-        out = {
-            "metric": "%s (batched render, exact coverage)" % unit, "value": value, "unit": unit,
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded generators), resident in HBM",
-            "config": run_config(args, specs, world),
-            "form": {"timed": "euc_graph replay" if form == "graph" else "euc_render_batch calls",
-                     "plain_value": world * args.scenes / (ms_plain / args.steps / 1e3),
-                     "graph_value": world * args.scenes / (ms_graph / args.steps / 1e3) if ms_graph else None,
-                     "tuning": tuning.as_dict() if tuning is not None else None, "autotune": tune_info},
-            "per_scene": {"value": per_scene, "unit": unit, "path": "euc_render per scene"},
-            "batched_speedup": value / world / per_scene if per_scene else None,
-            "mfrag_per_s": cand_per_step * world / (ms_step / 1e3) / 1e6,
-            "mtri_per_s": sum(f.ntris for f in specs) * world / (ms_step / 1e3) / 1e6,
-            "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()},
-            "gpu_launches": int(launches),
-            "roofline": {"bound": "hbm", "kernel": "k_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind,
-                         "algorithmic_bytes_per_launch": alg_bytes,
-                         # captured at the default workload sizes only
-                         "traffic": traffic.get(args.workload, {}).get("k_" + dom)
-                         if traffic and not args.frames and args.scenes == N_SCENES else None},
-            # the whole step (every stage, launch gaps included) against the same peak
-            "pipeline_roofline": {"achieved": alg_bytes / (ms_step / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
-                                  "frac": alg_bytes / (ms_step / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
-                                  "clear_bytes_per_step": clear_bytes,
-                                  "frac_with_clear": (alg_bytes + clear_bytes) / (ms_step / 1e3) / 1e9 / peak},
-            "e2e": {"value": e2e, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "path": "euc_render_host_batch (host buffers, blocking; one call per pass)",
-                    "host_copy": host_copy,
-                    "bytes": "host-buffer bytes each step's calls read (inputs, textures, targets) and write "
-                             "(targets); in place, only the covered pixels of a target cross the link",
-                    "per_scene_value": e2e_per_scene,
-                    "per_scene_path": "euc_render_host per scene (host buffers, blocking)"},
-            "cpu_baseline": cpu,
-            "clocks": clk,
-        }
-        print(json.dumps(out), flush=True)
+        def per_scene_pass():
+            batch.clear()
+            for a in calls:
+                rc = render(*a)
+                if rc != abi.OK:
+                    raise RuntimeError("euc_render failed: %d" % rc)
+        per_scene_pass()
+        capi.check(ctx.sync(sp), "per-scene warm-up")
+        t = timed(per_scene_pass, per_scene_reps)
+        per_scene = len(specs) / (t / per_scene_reps / 1e3)
+        ctx.set_tuning(tuned)
     if graph:
         graph.close()
-    ctx.close()
-    if world > 1:
-        dist.destroy_process_group()
+    alg = sum(f.algorithmic_bytes() for f in specs)
+    clear = sum(t.width * t.height * t.bpp for f in specs for t in f.targets)
+    return {"ms_step": ms / steps, "ms_plain_step": ms_plain / steps,
+            "ms_graph_step": ms_graph / steps if ms_graph else None, "form": form,
+            "stage_ms": {k: v / steps for k, v in stage_ms.items()},
+            "launches": int(graph_launches if form == "graph" else launches) // steps,
+            "cand": cand, "alg_bytes": alg, "clear_bytes": clear, "per_scene": per_scene,
+            "tuning": tuning.as_dict() if tuning is not None else None, "autotune": tune_info, "batch": batch}
 
 
-def run_serve(args):
+def rooflines(m, name, peak, peak_kind, clk_mhz):
+    """The HBM roofline of the dominant stage (algorithmic bytes over its
+    CUDA-event time; its kernels' measured DRAM bytes over the same time,
+    where a profile of this workload holds them), the whole step's HBM
+    fraction, and the issue-side roofline of the raster stage."""
+    stage = m["stage_ms"]
+    dom = max(stage, key=lambda k: stage[k])
+    dom_s = stage[dom] / 1e3
+    achieved = m["alg_bytes"] / dom_s / 1e9
+    traffic = load_profile_json("traffic.json") or {}
+    tw = traffic.get(name, {})
+    kb = [tw.get(k) for k in STAGE_KERNELS[dom]]
+    dram = sum(b for b in kb if b) if any(kb) else None
+    step_s = m["ms_step"] / 1e3
+    roof = {"bound": "hbm", "stage": dom, "kernels": STAGE_KERNELS[dom], "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": m["alg_bytes"],
+            "traffic": dram,
+            "dram_frac": (dram / dom_s / 1e9 / peak) if dram else None}
+    # issue side: candidate fragments per second against every issue slot of
+    # the GPU running full warps of the fewest instructions a candidate needs
+    rs = stage["raster"] / 1e3
+    sm_mhz = clk_mhz or 2070.0
+    peak_cand = 152 * 4 * sm_mhz * 1e6 * 32 / MIN_INST_PER_CANDIDATE
+    issue = {"stage": "raster", "candidates_per_step": m["cand"], "achieved": m["cand"] / rs, "peak": peak_cand,
+             "unit": "candidates/s", "frac": m["cand"] / rs / peak_cand,
+             "min_thread_inst_per_candidate": MIN_INST_PER_CANDIDATE, "sm_mhz": sm_mhz}
+    prof = (load_profile_json("issue.json") or {}).get(name)
+    if prof:
+        issue["ncu"] = prof
+    roof["issue"] = issue
+    pipe = {"achieved": m["alg_bytes"] / step_s / 1e9, "peak": peak, "unit": "GB/s",
+            "frac": m["alg_bytes"] / step_s / 1e9 / peak, "peak_kind": peak_kind,
+            "clear_bytes_per_step": m["clear_bytes"],
+            "frac_with_clear": (m["alg_bytes"] + m["clear_bytes"]) / step_s / 1e9 / peak}
+    return roof, pipe
+
+
+def serve_sweep(local, frames, rates, seconds, max_batch, slots, warmup, seed, rank=0):
     """The serving loop under open-loop Poisson arrivals, one run per rate.
-    Requests draw uniformly from a pool of `--scenes` seeded two-pass
-    requests over the resident meshes and textures; each run reports
-    latency percentiles (arrival to colour on the host) and throughput."""
-    import ctypes as C
-
+    Requests draw uniformly from a pool of seeded two-pass requests over the
+    resident meshes and textures; each run reports latency percentiles
+    (arrival to colour on the host) and throughput."""
     import torch
-    import torch.distributed as dist
     from euc_gb300 import abi, serve
 
-    world, rank, local = dist_env()
-    if world > 1:
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    torch.cuda.set_device(local)
-    frames = make_frames(args, rank)
-    srv = serve.Server(local, framebuffer_budget=40 << 30, max_batch=args.max_batch, slots=args.slots)
+    srv = serve.Server(local, framebuffer_budget=40 << 30, max_batch=max_batch, slots=slots)
     res = serve.Resident(srv)
     pins, keep, pool, outs = [], [], [], []
     for k, f in enumerate(frames):
@@ -581,31 +559,167 @@ def run_serve(args):
         pool.append(r)
         keep.append(kp)
     arr = (abi.ServerRequest * len(pool))(*pool)
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(max(warmup, 3)):
         # enough at once that every slot takes full batches: each slot's
         # scratch is sized before the timed runs
-        for _ in range(max(args.slots, 1)):
+        for _ in range(max(slots, 1)):
             srv.submit(arr)
         srv.drain()
         while len(srv.poll(8192)):
             pass
     base = srv.stats()
-    bus = None
-    try:
-        bus = torch.cuda.get_device_properties(local).pci_bus_id
-    except AttributeError:
-        pass
     runs = []
-    clocks = ClockSampler(bus)
-    clocks.start()
-    time.sleep(1.0)  # the sampler's start (NVML set-up) stays out of the first run
-    for i, rate in enumerate(float(r) for r in args.rates.split(",")):
-        _, summ = serve.run_poisson(srv, arr, outs, rate, args.serve_seconds, seed=args.seed + 17 * i + rank)
+    for i, rate in enumerate(rates):
+        _, summ = serve.run_poisson(srv, arr, outs, rate, seconds, seed=seed + 17 * i + rank)
         summ.pop("stats")
         runs.append(summ)
-    clk = clocks.stop()
     st = srv.stats()
     srv.close()
+    out_mean = float(np.mean([serve.out_bytes(f, ("color",)) for f in frames]))
+    return runs, int(st["launches"] - base["launches"]), out_mean
+
+
+def other_configs(args, ctx, dev, stream, peak, peak_kind):
+    """The other configurations, measured after the headline one in the
+    same process: the 640x480 sphere stream, the 1080p soup, the two-pass
+    knot (each batched and per scene), and a shortened serving sweep."""
+    from euc_gb300 import scenes
+    out = {}
+    plan = [("sphere", [scenes.sphere_frame(seed=i) for i in range(1024)], 5, "frames/s"),
+            ("soup", [scenes.soup_frame(seed=0)], 20, "frames/s"),
+            ("knot", [scenes.knot_frame(seed=i) for i in range(4)], 10, "frames/s")]
+    clocks = ClockSampler(_bus_id(dev))
+    clocks.start()
+    time.sleep(1.0)
+    for name, specs, steps, unit in plan:
+        m = measure(ctx, specs, dev, stream, steps, 3, tune=True, tune_reps=5, per_scene_reps=2)
+        rate = len(specs) / (m["ms_step"] / 1e3)
+        roof, pipe = rooflines(m, name, peak, peak_kind, None)
+        out[name] = {"workload": WORKLOADS[name][0], "frames_per_step": len(specs), "value": rate, "unit": unit,
+                     "form": m["form"], "plain_value": len(specs) / (m["ms_plain_step"] / 1e3),
+                     "per_scene": m["per_scene"], "batched_speedup": rate / m["per_scene"] if m["per_scene"] else None,
+                     "ms_per_step": m["ms_step"], "stage_ms_per_step": m["stage_ms"], "gpu_launches": m["launches"],
+                     "mfrag_per_s": m["cand"] / (m["ms_step"] / 1e3) / 1e6,
+                     "mtri_per_s": sum(f.ntris for f in specs) / (m["ms_step"] / 1e3) / 1e6,
+                     "tuning": m["tuning"], "roofline": roof, "pipeline_roofline": pipe}
+        del m
+    runs, launches, out_mean = serve_sweep(dev.index if hasattr(dev, "index") else 0,
+                                           make_frames(argparse.Namespace(workload="serve", seed=args.seed,
+                                                                          scenes=WORKLOADS["serve"][1]), 0),
+                                           [2000.0, 10000.0, 50000.0], args.serve_short_seconds, 256, 3, 3,
+                                           args.seed)
+    out["serve"] = {"workload": WORKLOADS["serve"][0], "unit": "requests/s", "seconds_per_rate": args.serve_short_seconds,
+                    "runs": runs, "gpu_launches": launches, "readback_bytes_per_request": out_mean}
+    out["clocks"] = clocks.stop()
+    return out
+
+
+def _bus_id(dev):
+    import torch
+    try:
+        return torch.cuda.get_device_properties(dev).pci_bus_id
+    except AttributeError:
+        return None
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+    from euc_gb300 import capi
+
+    world, rank, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    specs = make_frames(args, rank)
+    ctx = capi.Context(local)
+    stream = torch.cuda.current_stream()
+    peak, peak_kind = load_peaks()
+
+    clocks = ClockSampler(_bus_id(dev))
+    clocks.start()
+    time.sleep(0.3)
+    m = measure(ctx, specs, dev, stream, args.steps, args.warmup, tune=not args.no_tune, graph_ok=not args.no_graph,
+                world=world, per_scene_reps=0 if args.only_batched else max(2, args.steps // 4))
+    clk = clocks.stop()
+    value = world * args.scenes / (m["ms_step"] / 1e3)
+    e2e = e2e_per_scene = None
+    if not args.only_batched:
+        e2e_per_scene = run_e2e(ctx, specs, reps=1)
+        e2e = run_e2e_batch(ctx, specs, reps=max(2, min(args.steps, 5)))
+    h2d, d2h = host_bytes(specs)
+    host_copy = ("in place: kernels read vertices and indices and update targets in host memory over "
+                 "NVLink-C2C; one kernel gathers the textures") if ctx.host_copy_direct() else \
+        "staged through page-locked memory by host threads, one copy each way"
+    roof, pipe = rooflines(m, args.workload if not args.frames and args.scenes == WORKLOADS[args.workload][1]
+                           else "", peak, peak_kind, clk.get("sm_mhz"))
+    cpu = None
+    if rank == 0 and not args.no_baseline and not args.only_batched:
+        n, t, threads = cpu_sample(specs, args.cpu_seconds)
+        cpu = {"value": n / t, "unit": WORKLOADS[args.workload][2], "cores": threads, "kind": "port",
+               "sample": "%d scenes (rotating through the %d of one step) in %.1f s (oracle render_par, %d threads)"
+                         % (n, len(specs), t, threads)}
+    others = None
+    if args.workload == "batch" and not args.only_batched and not args.no_extras and world == 1:
+        del m["batch"]
+        others = other_configs(args, ctx, dev, stream, peak, peak_kind)
+    if rank == 0:
+        unit = WORKLOADS[args.workload][2]
+        out = {
+            "metric": "%s (batched render, exact coverage)" % unit, "value": value, "unit": unit,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": m["ms_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generators), resident in HBM",
+            "config": run_config(args, specs, world),
+            "form": {"timed": "euc_graph replay" if m["form"] == "graph" else "euc_render_batch calls",
+                     "plain_value": world * args.scenes / (m["ms_plain_step"] / 1e3),
+                     "graph_value": world * args.scenes / (m["ms_graph_step"] / 1e3) if m["ms_graph_step"] else None,
+                     "tuning": m["tuning"], "autotune": m["autotune"]},
+            "per_scene": {"value": m["per_scene"], "unit": unit,
+                          "path": "euc_render per scene pass, arguments built once"},
+            "batched_speedup": value / world / m["per_scene"] if m["per_scene"] else None,
+            "mfrag_per_s": m["cand"] * world / (m["ms_step"] / 1e3) / 1e6,
+            "mtri_per_s": sum(f.ntris for f in specs) * world / (m["ms_step"] / 1e3) / 1e6,
+            "stage_ms_per_step": m["stage_ms"],
+            "gpu_launches": m["launches"] * args.steps,
+            "roofline": roof,
+            "pipeline_roofline": pipe,
+            "e2e": {"value": e2e, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "path": "euc_render_host_batch (host buffers, blocking; one call per pass)",
+                    "host_copy": host_copy,
+                    "bytes": "host-buffer bytes each step's calls read (inputs, textures, targets) and write "
+                             "(targets); in place, only the covered pixels of a target cross the link",
+                    "per_scene_value": e2e_per_scene,
+                    "per_scene_path": "euc_render_host per scene (host buffers, blocking)"},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        if others is not None:
+            out["other_configs"] = others
+        print(json.dumps(out), flush=True)
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_serve(args):
+    """--workload serve: the serving loop alone, at --rates for --serve-seconds each."""
+    import torch
+    import torch.distributed as dist
+
+    world, rank, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    frames = make_frames(args, rank)
+    clocks = ClockSampler(_bus_id(torch.device("cuda", local)))
+    clocks.start()
+    time.sleep(1.0)  # the sampler's start (NVML set-up) stays out of the first run
+    runs, launches, out_mean = serve_sweep(local, frames, [float(r) for r in args.rates.split(",")],
+                                           args.serve_seconds, args.max_batch, args.slots, args.warmup,
+                                           args.seed, rank)
+    clk = clocks.stop()
     top = runs[-1]
     tot = [torch.tensor([r["throughput"]], device="cuda:%d" % local) for r in runs]
     if world > 1:
@@ -614,20 +728,19 @@ def run_serve(args):
         dist.destroy_process_group()
     if rank == 0:
         desc, _, unit = WORKLOADS["serve"]
-        per_req_out = float(np.mean([serve.out_bytes(f, ("color",)) for f in frames]))
         out = {
             "metric": "served requests/s with p50/p99 latency (arrival to colour on host)", "value": float(tot[-1].item()),
             "unit": unit, "n_gpus": world, "steps": len(runs), "warmup": max(args.warmup, 3),
             "ms_per_step": 1e3 * args.serve_seconds, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators), meshes/textures resident",
             "config": {"workload": desc, "name": "serve", "pool": len(frames), "seed": args.seed,
-                       "rates": args.rates, "seconds_per_rate": args.serve_seconds, "max_batch": args.max_batch, "slots": args.slots,
-                       "parallelism": "replicas" if world > 1 else "1 GPU"},
+                       "rates": args.rates, "seconds_per_rate": args.serve_seconds, "max_batch": args.max_batch,
+                       "slots": args.slots, "parallelism": "replicas" if world > 1 else "1 GPU"},
             "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
             "serving": runs,
-            "gpu_launches": int(st["launches"] - base["launches"]),
+            "gpu_launches": launches,
             "e2e": {"value": float(tot[-1].item()), "unit": unit, "h2d_bytes_per_step": None,
-                    "d2h_bytes_per_step": per_req_out * top["completed"],
+                    "d2h_bytes_per_step": out_mean * top["completed"],
                     "path": "euc_server_submit -> completion with colour in pinned host memory"},
             "roofline": None, "cpu_baseline": None, "clocks": clk,
         }
