@@ -71,6 +71,11 @@ struct euc_ctx {
     size_t ev_used = 0;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_marks;
     uint64_t launches = 0;
+    // euc_render's recorded shapes (render_one), and how often each shape
+    // was seen before it is recorded
+    std::vector<struct ShapeGraph *> shapes;
+    std::map<std::vector<unsigned char>, int> sightings;
+    uint64_t shape_clock = 0;
     std::mutex mu;
 };
 
@@ -476,6 +481,8 @@ void dispatch_resolve_ordered(uint32_t shader, const SceneDev *sc, const uint64_
 // stream is synchronised and the ordered path (which synchronises) is refused.
 struct StageOverride {
     bool dry = false;
+    bool fill = false;     // fill `host` with the scene tables and return: nothing is enqueued
+    bool no_copy = false;  // enqueue the launches without the copy of `host` to `dev`
     void *host = nullptr;
     void *dev = nullptr;
     size_t need = 0;
@@ -624,7 +631,8 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
         hrb[i] = res_base[i];
         hgb[i] = gin_base[i];
     }
-    CUDA_TRY(cudaMemcpyAsync(dv, h, off_u, cudaMemcpyHostToDevice, st));
+    if (so && so->fill) return EUC_OK;
+    if (!so || !so->no_copy) CUDA_TRY(cudaMemcpyAsync(dv, h, off_u, cudaMemcpyHostToDevice, st));
     const SceneDev *dsc = (const SceneDev *)(dv + off_sc);
     const uint64_t *dvb = (const uint64_t *)(dv + off_vb), *drb = (const uint64_t *)(dv + off_rb),
                    *dgb = (const uint64_t *)(dv + off_gb), *dsb = (const uint64_t *)(dv + off_sb);
@@ -770,6 +778,11 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
 
 }  // namespace
 
+namespace {
+int render_one(euc_ctx *ctx, const euc_scene &s, cudaStream_t st);
+void free_shapes(euc_ctx *ctx);
+}  // namespace
+
 extern "C" {
 
 int euc_abi_version(void) { return EUC_ABI_VERSION; }
@@ -823,6 +836,7 @@ int euc_ctx_destroy(euc_ctx *ctx) {
     if (!ctx) return EUC_ERR_INVALID;
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
+    free_shapes(ctx);
     DevBuf *bufs[] = {&ctx->clip, &ctx->vdata, &ctx->recs, &ctx->rows, &ctx->chunk_sums, &ctx->live_tri, &ctx->live_rowoff,
                       &ctx->totals, &ctx->vbuf, &ctx->err, &ctx->stats, &ctx->cov, &ctx->obsum, &ctx->frags,
                       &ctx->plan, &ctx->galive, &ctx->h_arena, &ctx->h_tex[0], &ctx->strip_cnt, &ctx->strip_fill,
@@ -965,7 +979,7 @@ int euc_render(euc_ctx *ctx, const euc_pipeline_desc *desc, const void *uniforms
     s.uniforms_size = uniforms_size;
     std::lock_guard<std::mutex> g(ctx->mu);
     CUDA_TRY(cudaSetDevice(ctx->device));
-    return run_batch(ctx, &s, 1, (cudaStream_t)stream);
+    return render_one(ctx, s, (cudaStream_t)stream);
 }
 
 int euc_render_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, void *stream) {
@@ -1007,6 +1021,184 @@ void graph_free(euc_graph *g) {
     if (g->host) cudaFreeHost(g->host);
     if (g->dev) cudaFree(g->dev);
     delete g;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// euc_render's recorded shapes.  A plain render is eight dependent stream
+// operations (the scene-table copy and seven launches), and for a small
+// scene their launch latencies, not the kernels, set the time per call.  So
+// euc_render records the launches of a scene shape as a CUDA graph the
+// second time it sees that shape, and from then on a call of the same shape
+// fills the scene table and uniforms into one of the shape's page-locked
+// staging slots, copies them to the shape's device staging and replays the
+// graph: one copy and one graph launch.  A shape is everything that decides
+// the launches and their arguments: the scene record without its buffer
+// pointers, the uniform size, the launch shape (euc_tuning), and the
+// context's scratch buffers (a render that moved them retires the shape's
+// graph).  Ordered-path scenes (which synchronise) and profiled renders stay
+// on the plain path.
+// ---------------------------------------------------------------------------
+constexpr int kShapeSlots = 4;     // staging slots of a recorded shape
+constexpr size_t kShapeCap = 512;  // recorded shapes of a context at most (least recently used go)
+constexpr size_t kSightCap = 4096; // shapes counted before the count starts over
+
+struct ShapeGraph {
+    std::vector<unsigned char> key;
+    void *scratch[kScratchBufs] = {};
+    unsigned char *host = nullptr;  // kShapeSlots staging slots of `stride` bytes
+    void *dev = nullptr;            // the staging the graph's kernels read
+    size_t need = 0, stride = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t slot_done[kShapeSlots] = {};
+    bool slot_pending[kShapeSlots] = {};
+    int next = 0;
+    cudaEvent_t done = nullptr;  // after the last replay
+    bool launched = false;
+    uint64_t launches = 0, last_use = 0;
+};
+
+namespace {
+
+void shape_free(ShapeGraph *g) {
+    if (g->launched) cudaEventSynchronize(g->done);
+    for (int k = 0; k < kShapeSlots; ++k)
+        if (g->slot_done[k]) cudaEventDestroy(g->slot_done[k]);
+    if (g->done) cudaEventDestroy(g->done);
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    if (g->host) cudaFreeHost(g->host);
+    if (g->dev) cudaFree(g->dev);
+    delete g;
+}
+
+void free_shapes(euc_ctx *ctx) {
+    for (ShapeGraph *g : ctx->shapes) shape_free(g);
+    ctx->shapes.clear();
+    ctx->sightings.clear();
+}
+
+std::vector<unsigned char> shape_key(const euc_ctx *ctx, const Plan &p) {
+    SceneDev d = p.d;  // plan_scene zeroed the padding
+    d.verts = nullptr;
+    d.idx = nullptr;
+    d.uniforms = nullptr;
+    d.pixel = nullptr;
+    d.depth = nullptr;
+    std::vector<unsigned char> k(sizeof(d) + sizeof(p.usize) + sizeof(euc_tuning));
+    std::memcpy(k.data(), &d, sizeof(d));
+    std::memcpy(k.data() + sizeof(d), &p.usize, sizeof(p.usize));
+    std::memcpy(k.data() + sizeof(d) + sizeof(p.usize), &ctx->tune, sizeof(euc_tuning));
+    return k;
+}
+
+// Records the launches of scene `s` as a new shape; nullptr when it cannot.
+ShapeGraph *shape_record(euc_ctx *ctx, const euc_scene &s, std::vector<unsigned char> key) {
+    StageOverride so;
+    so.dry = true;
+    if (run_batch(ctx, &s, 1, nullptr, &so)) return nullptr;  // validates, sizes the scratch
+    ShapeGraph *g = new (std::nothrow) ShapeGraph();
+    if (!g) return nullptr;
+    g->key = std::move(key);
+    g->need = std::max<size_t>(so.need, 256);
+    g->stride = pad_up(g->need, 256);
+    bool ok = cudaMallocHost((void **)&g->host, g->stride * kShapeSlots) == cudaSuccess &&
+              cudaMalloc(&g->dev, g->need) == cudaSuccess &&
+              cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming) == cudaSuccess;
+    for (int k = 0; ok && k < kShapeSlots; ++k)
+        ok = cudaEventCreateWithFlags(&g->slot_done[k], cudaEventDisableTiming) == cudaSuccess;
+    cudaStream_t cs = nullptr;
+    ok = ok && cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess;
+    if (ok && cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        so.dry = false;
+        so.no_copy = true;
+        so.host = g->host;
+        so.dev = g->dev;
+        so.need = g->need;
+        ctx->capturing = true;
+        const uint64_t l0 = ctx->launches;
+        const int rc = run_batch(ctx, &s, 1, cs, &so);
+        g->launches = ctx->launches - l0;
+        ctx->launches = l0;
+        ctx->capturing = false;
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(cs, &graph);
+        g->graph = graph;
+        ok = rc == EUC_OK && ec == cudaSuccess && graph &&
+             cudaGraphInstantiate(&g->exec, g->graph, 0) == cudaSuccess;
+    } else {
+        ok = false;
+    }
+    if (cs) cudaStreamDestroy(cs);
+    (void)cudaGetLastError();
+    if (!ok) {
+        shape_free(g);
+        return nullptr;
+    }
+    scratch_ptrs(ctx, g->scratch);
+    return g;
+}
+
+int render_one(euc_ctx *ctx, const euc_scene &s, cudaStream_t st) {
+    Plan p;
+    if (int rc = plan_scene(s, p)) return rc;
+    if (ctx->profiling || p.skip || p.d.keytype == KEY_ORDERED) return run_batch(ctx, &s, 1, st);
+    std::vector<unsigned char> key = shape_key(ctx, p);
+    ShapeGraph *g = nullptr;
+    size_t at = 0;
+    for (; at < ctx->shapes.size(); ++at)
+        if (ctx->shapes[at]->key == key) {
+            g = ctx->shapes[at];
+            break;
+        }
+    if (g) {
+        void *now[kScratchBufs];
+        scratch_ptrs(ctx, now);
+        if (std::memcmp(now, g->scratch, sizeof(now)) != 0) {  // the scratch moved: record again
+            shape_free(g);
+            ctx->shapes.erase(ctx->shapes.begin() + (long)at);
+            g = nullptr;
+        }
+    }
+    if (!g) {
+        if (ctx->sightings.size() >= kSightCap) ctx->sightings.clear();
+        if (++ctx->sightings[key] < 2) return run_batch(ctx, &s, 1, st);  // seen once: plain
+        if (ctx->shapes.size() >= kShapeCap) {  // make room: the least recently used goes
+            size_t lru = 0;
+            for (size_t i = 1; i < ctx->shapes.size(); ++i)
+                if (ctx->shapes[i]->last_use < ctx->shapes[lru]->last_use) lru = i;
+            shape_free(ctx->shapes[lru]);
+            ctx->shapes.erase(ctx->shapes.begin() + (long)lru);
+        }
+        g = shape_record(ctx, s, key);
+        if (!g) return run_batch(ctx, &s, 1, st);
+        ctx->shapes.push_back(g);
+    }
+    g->last_use = ++ctx->shape_clock;
+    const int k = g->next;
+    g->next = (k + 1) % kShapeSlots;
+    if (g->slot_pending[k]) {  // the slot's previous copy has been read
+        CUDA_TRY(cudaEventSynchronize(g->slot_done[k]));
+        g->slot_pending[k] = false;
+    }
+    unsigned char *slot = g->host + (size_t)k * g->stride;
+    StageOverride so;
+    so.fill = true;
+    so.host = slot;
+    so.dev = g->dev;
+    so.need = g->need;
+    if (int rc = run_batch(ctx, &s, 1, st, &so)) return rc;
+    if (g->launched) CUDA_TRY(cudaStreamWaitEvent(st, g->done, 0));  // a replay on another stream has finished
+    CUDA_TRY(cudaMemcpyAsync(g->dev, slot, g->need, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaEventRecord(g->slot_done[k], st));
+    g->slot_pending[k] = true;
+    CUDA_TRY(cudaGraphLaunch(g->exec, st));
+    CUDA_TRY(cudaEventRecord(g->done, st));
+    g->launched = true;
+    ctx->launches += g->launches;
+    return EUC_OK;
 }
 
 }  // namespace

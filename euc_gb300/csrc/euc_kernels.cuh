@@ -1215,6 +1215,14 @@ __global__ void __launch_bounds__(kBlock, 4) k_raster(const SceneDev *__restrict
     const int lane = threadIdx.x & 31;
     uint64_t *off = s_off[threadIdx.x >> 5];
     const uint64_t nlive = totals[0], nitems = totals[1];
+    // Few items for the grid (a small scene): smaller claims, down to one
+    // step, so that every warp gets some instead of a few warps walking
+    // many steps each (uniform over the grid: it depends on nitems alone)
+    {
+        const uint64_t nwarps = (uint64_t)gridDim.x * (kBlock / 32);
+        const uint64_t fair = (nitems + nwarps - 1) / nwarps;
+        if (fair < (uint64_t)witems) witems = (int)max((uint64_t)32, (fair + 31) / 32 * 32);
+    }
     // Warps beyond the number of chunks would only find the counter exhausted;
     // they leave at once instead of queueing on its atomic.
     const uint64_t gwarp = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5);
