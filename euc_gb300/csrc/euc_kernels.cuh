@@ -2004,7 +2004,6 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
     const bool win = inside && decode_key(s, vbuf[s.pix_base + (uint64_t)y * s.W + x], t, z);
     if (win && s.depth_write) *reinterpret_cast<float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x) = z;
     if (!s.pixel_write) return;  // uniform over the block (one scene)
-    if (!__syncthreads_or(win)) return;  // nothing to shade in this chunk
 
     // 2. the fragment evaluations this chunk needs, compacted into a job list.
     // A job is (pixel slot, corner); corner 0 is the pixel itself when there
@@ -2017,28 +2016,40 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
     uint32_t(*s_xy)[3] = sm.xy;
     uint16_t *s_job = sm.job;
     float(*s_frag)[4][F::NF] = sm.frag;
-    s_t[tid] = win ? t : 0xFFFFFFFFu;
+    const uint32_t tw = win ? t : 0xFFFFFFFFu;
+    s_t[tid] = tw;
     s_xy[tid][0] = x;
     s_xy[tid][1] = y;
     s_xy[tid][2] = lo;
-    __syncthreads();
+    if (!__syncthreads_or(win)) return;  // nothing to shade in this chunk (uniform); publishes s_t and s_xy
     const int own_c = (lane & 1) | ((lane >> 4) << 1);
+    // the winners of this pixel's 2x2 cell: a cell never leaves its warp's 16x2 tile
+    uint32_t nb[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) nb[c] = __shfl_sync(0xFFFFFFFFu, tw, (lane & ~17) | (c & 1) | ((c >> 1) << 4));
     uint32_t need = 0;  // bit c: this pixel evaluates corner c itself
     if (win) {
         if (s.level == 0) {
             need = 1u;
         } else if (quads) {
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const int owner = (tid & ~31) | (lane & ~17) | (c & 1) | ((c >> 1) << 4);
-                if (c == own_c || s_t[owner] != t) need |= 1u << c;
-            }
+            for (int c = 0; c < 4; ++c)
+                if (c == own_c || nb[c] != t) need |= 1u << c;
         } else {
             need = 0xFu;
         }
     }
-    uint32_t njobs;
-    uint32_t off = block_excl_scan<uint32_t>(__popc(need), sm.scan, &njobs);
+    // job offsets: the warp's prefix plus the totals of the warps before it
+    const uint32_t cnt = __popc(need), inc = warp_incl_scan(cnt);
+    if (lane == 31) sm.scan[tid >> 5] = inc;
+    __syncthreads();
+    uint32_t off = inc - cnt, njobs = 0;
+#pragma unroll
+    for (int w = 0; w < kBlock / 32; ++w) {
+        const uint32_t v = sm.scan[w];
+        off += w < (tid >> 5) ? v : 0u;
+        njobs += v;
+    }
 #pragma unroll
     for (int c = 0; c < 4; ++c)
         if (need & (1u << c)) s_job[off++] = (uint16_t)((tid << 2) | c);
@@ -2094,7 +2105,7 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
 // [s_begin, s_end); rbase (global scene index, from plan_chunks) holds the first
 // chunk of each.
 template <class F>
-__global__ void __launch_bounds__(kBlock) k_resolve(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ rbase,
+__global__ void __launch_bounds__(kBlock, 4) k_resolve(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ rbase,
                                                     int s_begin, int s_end, uint32_t group,
                                                     const TriRec *__restrict__ recs, const float *__restrict__ vdata,
                                                     const unsigned long long *__restrict__ vbuf,
