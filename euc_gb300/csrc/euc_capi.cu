@@ -699,7 +699,7 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
                                            (const uint4 *)ctx->cov.p, (const SceneStats *)ctx->stats.p,
                                            (const uint32_t *)ctx->strip_off.p, (uint32_t *)ctx->strip_fill.p,
                                            (uint2 *)ctx->entries.p, strip_mode);
-        k_strip<<<(unsigned)ctx->nsm * 2, kStripThreads, strip_smem, st>>>(
+        k_strip<<<(unsigned)ctx->nsm * kStripBlocksPerSm, kStripThreads, strip_smem, st>>>(
             dsc, dsb, ns, (const uint4 *)ctx->cov.p, (const uint32_t *)ctx->strip_off.p,
             (const uint32_t *)ctx->strip_uoff.p, (const uint32_t *)ctx->unit_strip.p, (const uint2 *)ctx->entries.p,
             (const TriRec *)ctx->recs.p, (const int *)ctx->err.p, (unsigned long long *)ctx->vbuf.p,

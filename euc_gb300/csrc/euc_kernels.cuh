@@ -542,6 +542,7 @@ constexpr uint32_t kTinyPixels = 4;
 // primitive goes changes no result: the keys are order-free reductions.
 // ---------------------------------------------------------------------------
 constexpr int kStripThreads = 512;            // threads of a k_strip block
+constexpr int kStripBlocksPerSm = 2;          // k_strip blocks resident per SM (its grid)
 constexpr uint32_t kStripMaxRows = 16;        // rows of a strip at most
 constexpr size_t kStripKeyBytes = 96 * 1024;  // a strip's keys in shared memory at most
 constexpr uint32_t kRowsBinned = 0x80000000u; // rows[t]: the primitive went to the strips
@@ -564,7 +565,7 @@ __host__ __device__ inline uint32_t strip_rows(uint32_t W, uint32_t H) {
 }
 
 // Width bucket of a k_strip entry (its bbox width w): exact below 32, then
-// 16 pixels wide; entries are walked bucket by bucket.
+// 16 pixels wide; entries are walked bucket by bucket, widest first.
 constexpr uint32_t kWidthBuckets = 64;
 __host__ __device__ inline uint32_t width_bucket(uint32_t w) {
     return w < 32u ? w : (32u + ((w - 32u) >> 4) < kWidthBuckets - 1 ? 32u + ((w - 32u) >> 4) : kWidthBuckets - 1);
@@ -1508,7 +1509,7 @@ EUC_DEV uint32_t strip_block_scan(uint32_t v, uint32_t *smem /* >= kStripThreads
 // walk them with shared-memory reductions; every key the unit lowered is
 // then merged into vbuf (which k_init seeded) with one 64-bit min.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kStripThreads, 2) k_strip(const SceneDev *__restrict__ sc,
+__global__ void __launch_bounds__(kStripThreads, kStripBlocksPerSm) k_strip(const SceneDev *__restrict__ sc,
                                                             const uint64_t *__restrict__ sbase, int nsc,
                                                             const uint4 *__restrict__ cov,
                                                             const uint32_t *__restrict__ strip_off,
@@ -1555,9 +1556,10 @@ __global__ void __launch_bounds__(kStripThreads, 2) k_strip(const SceneDev *__re
         const uint32_t pitch = strip_pitch(wc);
         const uint32_t e_begin = strip_off[g] + (u - strip_uoff[g]) * kStripUnit;
         const int nload = (int)(min(e_begin + kStripUnit, strip_off[g + 1]) - e_begin);
-        // the unit's entries, two per thread, ordered by bbox width (a
-        // counting sort over kWidthBuckets), so that the rows a warp walks
-        // together have about the same length
+        // the unit's entries, two per thread, ordered by bbox width, widest
+        // first (a counting sort over kWidthBuckets): the rows a warp walks
+        // together have about the same length, and the short ones come last,
+        // so that the warps reach the unit's closing barrier together
         if (tid < (int)kWidthBuckets) s_bkt[tid] = 0;
         uint2 ev[2];
         uint32_t bk[2], rk[2];
@@ -1570,7 +1572,7 @@ __global__ void __launch_bounds__(kStripThreads, 2) k_strip(const SceneDev *__re
             if (k < nload) {
                 ev[h] = entries[e_begin + k];
                 const uint2 bx = __ldg(reinterpret_cast<const uint2 *>(recs + ev[h].x) + 6);  // bx0, bx1
-                bk[h] = width_bucket(bx.y - bx.x);
+                bk[h] = kWidthBuckets - 1u - width_bucket(bx.y - bx.x);  // widest first
             }
             const uint32_t m = __match_any_sync(0xFFFFFFFFu, bk[h]);
             const int leader = __ffs(m) - 1;
