@@ -564,8 +564,9 @@ __host__ __device__ inline uint32_t strip_rows(uint32_t W, uint32_t H) {
     return (uint32_t)(r < kStripMaxRows ? r : kStripMaxRows);
 }
 
-// Width bucket of a k_strip entry (its bbox width w): exact below 32, then
-// 16 pixels wide; entries are walked bucket by bucket, widest first.
+// Width bucket of a k_strip entry (the span w of its middle row in the
+// strip): exact below 32, then 16 pixels wide; entries are walked bucket by
+// bucket, widest first.
 constexpr uint32_t kWidthBuckets = 64;
 __host__ __device__ inline uint32_t width_bucket(uint32_t w) {
     return w < 32u ? w : (32u + ((w - 32u) >> 4) < kWidthBuckets - 1 ? 32u + ((w - 32u) >> 4) : kWidthBuckets - 1);
@@ -1556,10 +1557,11 @@ __global__ void __launch_bounds__(kStripThreads, kStripBlocksPerSm) k_strip(cons
         const uint32_t pitch = strip_pitch(wc);
         const uint32_t e_begin = strip_off[g] + (u - strip_uoff[g]) * kStripUnit;
         const int nload = (int)(min(e_begin + kStripUnit, strip_off[g + 1]) - e_begin);
-        // the unit's entries, two per thread, ordered by bbox width, widest
-        // first (a counting sort over kWidthBuckets): the rows a warp walks
-        // together have about the same length, and the short ones come last,
-        // so that the warps reach the unit's closing barrier together
+        // the unit's entries, two per thread, ordered by the span of their
+        // middle row in the strip, widest first (a counting sort over
+        // kWidthBuckets): the rows a warp walks together have about the same
+        // length, and the short ones come last, so that the warps reach the
+        // unit's closing barrier together
         if (tid < (int)kWidthBuckets) s_bkt[tid] = 0;
         uint2 ev[2];
         uint32_t bk[2], rk[2];
@@ -1571,8 +1573,15 @@ __global__ void __launch_bounds__(kStripThreads, kStripBlocksPerSm) k_strip(cons
             bk[h] = 0xFFFFFFFFu;
             if (k < nload) {
                 ev[h] = entries[e_begin + k];
-                const uint2 bx = __ldg(reinterpret_cast<const uint2 *>(recs + ev[h].x) + 6);  // bx0, bx1
-                bk[h] = kWidthBuckets - 1u - width_bucket(bx.y - bx.x);  // widest first
+                // the span of the entry's middle row in this strip: the bbox
+                // width where every row spans it, else the edge intersections
+                TriRec rs = load_rec(recs + ev[h].x, 0x38u);  // words 3-5
+                uint32_t xs = rs.bx0, xe = rs.bx1;
+                if (!(rs.flags & 2u)) {
+                    const uint32_t ya = ev[h].y >> 16, yb = ev[h].y & 0xFFFFu;
+                    if (!row_span(s, rs, s0 + ((ya + yb) >> 1), xs, xe)) xe = xs;
+                }
+                bk[h] = kWidthBuckets - 1u - width_bucket(xe - xs);  // widest first
             }
             const uint32_t m = __match_any_sync(0xFFFFFFFFu, bk[h]);
             const int leader = __ffs(m) - 1;
