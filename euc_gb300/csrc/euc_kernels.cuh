@@ -1925,13 +1925,14 @@ __global__ void __launch_bounds__(kBlock) k_prep(int *__restrict__ err, SceneSta
     if (i < 2) totals[6 + i] = 0;
 }
 
+// One warp's job list in k_resolve: its 32 pixels' winners and positions,
+// their fragment evaluations and the results.
 template <class F>
 struct ResolveSmem {
-    uint32_t t[kBlock];
-    uint32_t xy[kBlock][3];
-    uint16_t job[4 * kBlock];
-    float frag[kBlock][4][F::NF];
-    uint32_t scan[kBlock / 32 + 1];
+    uint32_t t[32];
+    uint32_t xy[32][3];
+    uint16_t job[4 * 32];
+    float frag[32][4][F::NF];
 };
 
 // Chunk `lb` of a resolve_direct scene: kBlock * kDirectPer pixels of the
@@ -2028,11 +2029,11 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
     uint16_t *s_job = sm.job;
     float(*s_frag)[4][F::NF] = sm.frag;
     const uint32_t tw = win ? t : 0xFFFFFFFFu;
-    s_t[tid] = tw;
-    s_xy[tid][0] = x;
-    s_xy[tid][1] = y;
-    s_xy[tid][2] = lo;
-    if (!__syncthreads_or(win)) return;  // nothing to shade in this chunk (uniform); publishes s_t and s_xy
+    if (!__any_sync(0xFFFFFFFFu, win)) return;  // nothing to shade in this warp's pixels
+    s_t[lane] = tw;
+    s_xy[lane][0] = x;
+    s_xy[lane][1] = y;
+    s_xy[lane][2] = lo;
     const int own_c = (lane & 1) | ((lane >> 4) << 1);
     // the winners of this pixel's 2x2 cell: a cell never leaves its warp's 16x2 tile
     uint32_t nb[4];
@@ -2050,27 +2051,20 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
             need = 0xFu;
         }
     }
-    // job offsets: the warp's prefix plus the totals of the warps before it
+    // the warp's job list
     const uint32_t cnt = __popc(need), inc = warp_incl_scan(cnt);
-    if (lane == 31) sm.scan[tid >> 5] = inc;
-    __syncthreads();
-    uint32_t off = inc - cnt, njobs = 0;
-#pragma unroll
-    for (int w = 0; w < kBlock / 32; ++w) {
-        const uint32_t v = sm.scan[w];
-        off += w < (tid >> 5) ? v : 0u;
-        njobs += v;
-    }
+    uint32_t off = inc - cnt;
+    const uint32_t njobs = __shfl_sync(0xFFFFFFFFu, inc, 31);
 #pragma unroll
     for (int c = 0; c < 4; ++c)
-        if (need & (1u << c)) s_job[off++] = (uint16_t)((tid << 2) | c);
-    __syncthreads();
+        if (need & (1u << c)) s_job[off++] = (uint16_t)((lane << 2) | c);
+    __syncwarp();
 
     // 3. every thread evaluates jobs until the list is done
     const typename F::U &u = *reinterpret_cast<const typename F::U *>(s.uniforms);
     const float *vb = vdata + (s.geom ? s.gvd_base : s.vd_base);
     const uint32_t L = s.level;
-    for (uint32_t j = tid; j < njobs; j += kBlock) {
+    for (uint32_t j = lane; j < njobs; j += 32) {
         const int slot = s_job[j] >> 2, c = s_job[j] & 3;
         const TriRec &r = recs[s_t[slot]];  // (field loads here: the vector copy costs this path registers)
         float xf, yf;
@@ -2086,19 +2080,19 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
         vdata_at<F>(s, r, vb, xf, yf, vd);
         F::fragment(u, vd, s_frag[slot][c]);
     }
-    __syncthreads();
+    __syncwarp();
 
     // 4. combine (pipeline.rs:541-573) and store
     if (!win) return;
     float frag[F::NF];
     if (L == 0) {
 #pragma unroll
-        for (int i = 0; i < F::NF; ++i) frag[i] = s_frag[tid][0][i];
+        for (int i = 0; i < F::NF; ++i) frag[i] = s_frag[lane][0][i];
     } else {
         int src[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c)
-            src[c] = (need & (1u << c)) ? tid : ((tid & ~31) | (lane & ~17) | (c & 1) | ((c >> 1) << 4));
+            src[c] = (need & (1u << c)) ? lane : ((lane & ~17) | (c & 1) | ((c >> 1) << 4));
         const float div = 1.0f / (float)(1u << L);
         const float fx = rfract((float)x * div);
         const float fy = rfract((float)(y - lo) * div);
@@ -2121,17 +2115,15 @@ __global__ void __launch_bounds__(kBlock, 4) k_resolve(const SceneDev *__restric
                                                     const TriRec *__restrict__ recs, const float *__restrict__ vdata,
                                                     const unsigned long long *__restrict__ vbuf,
                                                     const uint4 *__restrict__ cov) {
-    __shared__ ResolveSmem<F> sm;
-    __shared__ int s_scene;
+    // warps work independently: each has its own job list and no block barrier
+    __shared__ ResolveSmem<F> s_warp[kBlock / 32];
+    ResolveSmem<F> &sm = s_warp[threadIdx.x >> 5];
     const uint64_t *base = rbase + s_begin;
     const int n = s_end - s_begin;
     const uint64_t c_begin = base[0], c_end = base[n];
     for (uint64_t g = blockIdx.x; c_begin + g * group < c_end; g += gridDim.x) {
         const uint64_t c0 = c_begin + g * group;
-        __syncthreads();
-        if (threadIdx.x == 0) s_scene = find_scene(base, n, c0);
-        __syncthreads();
-        int si = s_scene;
+        int si = find_scene(base, n, c0);
         for (uint64_t c = c0; c < c0 + group && c < c_end; ++c) {
             si = advance_scene(base, n, si, c);
             const SceneDev &s = sc[s_begin + si];
@@ -2139,7 +2131,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_resolve(const SceneDev *__restric
                 resolve_direct_chunk<F>(s, cov[s_begin + si], c - base[si], recs, vdata, vbuf);
             } else {
                 resolve_chunk<F>(s, cov[s_begin + si], c - base[si], recs, vdata, vbuf, sm);
-                __syncthreads();  // the next chunk reuses shared memory
+                __syncwarp();  // the next chunk reuses the warp's shared memory
             }
         }
     }

@@ -216,11 +216,32 @@ CASES = {
 }
 
 
+_ORACLE = {}
+
+
+def _oracle(name):
+    """The oracle's targets and statistics of case `name`, computed once."""
+    if name not in _ORACLE:
+        _ORACLE[name] = run_oracle(CASES[name][0]())
+    return _ORACLE[name]
+
+
+@pytest.fixture(scope="module")
+def strip_ctx():
+    """A context that sends every scene the shared-memory strips can take to
+    them, whatever its overdraw (the default routes only overdrawn scenes)."""
+    from euc_gb300 import capi
+    ctx = capi.Context(0)
+    ctx.set_tuning(strip_path=2)
+    yield ctx
+    ctx.close()
+
+
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_gpu_matches_oracle(name, gpu_ctx):
     make, tol = CASES[name]
     assert_same_inputs(make(), make())
-    ref, ref_stats = run_oracle(make())
+    ref, ref_stats = _oracle(name)
     got, got_stats = run_gpu(gpu_ctx, make())
     assert [s[0] for s in got_stats] == [s[0] for s in ref_stats]
     assert [s[1] for s in got_stats] == [s[1] for s in ref_stats], "candidate fragment counts"
@@ -228,14 +249,27 @@ def test_gpu_matches_oracle(name, gpu_ctx):
     assert_targets_match(make(), ref, got, color_tol=tol)
 
 
-def test_index_out_of_bounds_draws_nothing(gpu_ctx):
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_gpu_matches_oracle_on_the_strips(name, strip_ctx):
+    make, tol = CASES[name]
+    ref, ref_stats = _oracle(name)
+    got, got_stats = run_gpu(strip_ctx, make())
+    assert [s[0] for s in got_stats] == [s[0] for s in ref_stats]
+    assert [s[1] for s in got_stats] == [s[1] for s in ref_stats], "candidate fragment counts"
+    assert [s[2] for s in got_stats] == [s[2] for s in ref_stats], "culled primitive counts"
+    assert_targets_match(make(), ref, got, color_tol=tol)
+
+
+@pytest.mark.parametrize("strips", [False, True])
+def test_index_out_of_bounds_draws_nothing(gpu_ctx, strip_ctx, strips):
+    ctx = strip_ctx if strips else gpu_ctx
     def make():
         f = scenes.sphere_frame(seed=1, width=120, height=90, lon=12, lat=6)
         f.passes[0].indices = f.passes[0].indices.copy()
         f.passes[0].indices[-1] = f.passes[0].nverts  # one past the end: index.rs:53 panics
         return f
     ref, ref_stats = run_oracle(make())
-    got, got_stats = run_gpu(gpu_ctx, make())
+    got, got_stats = run_gpu(ctx, make())
     assert ref_stats[0][0] == abi.ERR_INDEX_OOB
     assert got_stats[0][0] == abi.ERR_INDEX_OOB
     clean = make().alloc_host_targets()
