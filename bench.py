@@ -89,6 +89,8 @@ def parse():
                          "fill-rate and two-pass configurations, --frames of them per step")
     ap.add_argument("--frames", type=int, default=0, help="frames per step for sphere/soup/knot (0 = default)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape (no autotuning)")
+    ap.add_argument("--tuning", default=None,
+                    help='fixed launch shape instead of autotuning, as JSON fields of euc_tuning, e.g. \'{"strip_path": 2}\'')
     ap.add_argument("--no-graph", action="store_true", help="time plain euc_render_batch calls only")
     ap.add_argument("--rates", default="2000,10000,50000", help="serve: Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="serve: length of each rate's run")
@@ -410,7 +412,8 @@ def prebuilt_render_calls(ctx, batch, sp):
     return calls
 
 
-def measure(ctx, specs, dev, stream, steps, warmup, tune, graph_ok=True, world=1, tune_reps=9, per_scene_reps=2):
+def measure(ctx, specs, dev, stream, steps, warmup, tune, graph_ok=True, world=1, tune_reps=9, per_scene_reps=2,
+            fixed_tuning=None):
     """One workload on the GPU: the batched form (plain calls with per-stage
     CUDA events, and the recorded graph), the candidate count of one step,
     and the plain per-scene path (euc_render per scene pass, arguments built
@@ -425,7 +428,11 @@ def measure(ctx, specs, dev, stream, steps, warmup, tune, graph_ok=True, world=1
         fr.render_batch(ctx, batch, stream, clear=True)
 
     tuning, tune_info = None, None
-    if tune:
+    if fixed_tuning:
+        tuning = abi.Tuning(**fixed_tuning)
+        ctx.set_tuning(tuning)
+        tune_info = {"fixed": fixed_tuning}
+    elif tune:
         from euc_gb300 import autotune
         tuning, tune_info = autotune.tune(ctx, batch, stream, reps=tune_reps)
     graph = None
@@ -642,6 +649,7 @@ def run_gpu(args):
     clocks.start()
     time.sleep(0.3)
     m = measure(ctx, specs, dev, stream, args.steps, args.warmup, tune=not args.no_tune, graph_ok=not args.no_graph,
+                fixed_tuning=json.loads(args.tuning) if args.tuning else None,
                 world=world, per_scene_reps=0 if args.only_batched else max(2, args.steps // 4))
     clk = clocks.stop()
     value = world * args.scenes / (m["ms_step"] / 1e3)

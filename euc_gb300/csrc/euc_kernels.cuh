@@ -1419,6 +1419,33 @@ EUC_DEV void smem_min_u64(uint32_t saddr, unsigned long long v) {
     asm volatile("red.shared.min.u64 [%0], %1;" ::"r"(saddr), "l"(v) : "memory");
 }
 
+// The KEY_MIN walk of strip_walk_row, with the clip-range test compiled in
+// or out (a record's flag bit 0: the whole triangle lies inside [zmin, zmax]).
+template <bool kClip>
+EUC_DEV void strip_walk_min(float w0, float w1, float w2, float d0, float d1, float d2, float z0, float z1, float z2,
+                            float zmin, float zmax, uint32_t flip, uint32_t tmin, uint32_t xs, uint32_t xe,
+                            uint32_t srow, uint32_t &cnt) {
+#pragma unroll 4
+    for (uint32_t x = xs; x < xe; ++x) {
+        const float wu2 = (w2 - w0) - w1;
+        if (w0 >= 0.0f && w1 >= 0.0f && wu2 >= 0.0f) {
+            const float z = (z0 * w0 + z1 * w1) + z2 * wu2;
+            if (!kClip || (zmin <= z && z <= zmax)) {
+                ++cnt;
+                if (z == z) {  // a NaN depth fails every test (partial_cmp is None)
+                    const uint32_t b = __float_as_uint(z + 0.0f);  // -0 and +0 compare equal
+                    const uint32_t o = (b ^ ((uint32_t)((int32_t)b >> 31) | 0x80000000u)) ^ flip;
+                    const uint32_t neg0 = __float_as_uint(z) == 0x80000000u ? 1u : 0u;
+                    smem_min_u64(srow + 8u * x, ((unsigned long long)o << 32) | (tmin | neg0));
+                }
+            }
+        }
+        w0 = w0 + d0;
+        w1 = w1 + d1;
+        w2 = w2 + d2;
+    }
+}
+
 // walk_row for a strip: the same serial walk (triangles.rs:257-301), with
 // the keys in shared memory; `srow` is the shared address of the row's key
 // for x = 0 (8 bytes per pixel).  KEY_MIN or KEY_LAST scenes.
@@ -1436,25 +1463,10 @@ EUC_DEV void strip_walk_row(const SceneDev &s, const TriRec &r, uint32_t t, uint
     if (s.keytype == KEY_MIN) {
         const uint32_t flip = s.depth_test == EUC_TEST_GREATER ? 0xFFFFFFFFu : 0u;
         const uint32_t tmin = (t + 1u) << 1;
-#pragma unroll 4
-        for (uint32_t x = xs; x < xe; ++x) {
-            const float wu2 = (w2 - w0) - w1;
-            if (w0 >= 0.0f && w1 >= 0.0f && wu2 >= 0.0f) {
-                const float z = (z0 * w0 + z1 * w1) + z2 * wu2;
-                if (noclip || (zmin <= z && z <= zmax)) {
-                    ++cnt;
-                    if (z == z) {  // a NaN depth fails every test (partial_cmp is None)
-                        const uint32_t b = __float_as_uint(z + 0.0f);  // -0 and +0 compare equal
-                        const uint32_t o = (b ^ ((uint32_t)((int32_t)b >> 31) | 0x80000000u)) ^ flip;
-                        const uint32_t neg0 = __float_as_uint(z) == 0x80000000u ? 1u : 0u;
-                        smem_min_u64(srow + 8u * x, ((unsigned long long)o << 32) | (tmin | neg0));
-                    }
-                }
-            }
-            w0 = w0 + d0;
-            w1 = w1 + d1;
-            w2 = w2 + d2;
-        }
+        if (noclip)
+            strip_walk_min<false>(w0, w1, w2, d0, d1, d2, z0, z1, z2, zmin, zmax, flip, tmin, xs, xe, srow, cnt);
+        else
+            strip_walk_min<true>(w0, w1, w2, d0, d1, d2, z0, z1, z2, zmin, zmax, flip, tmin, xs, xe, srow, cnt);
         return;
     }
     // KEY_LAST: every fragment against the unchanged initial depth
@@ -1508,7 +1520,8 @@ EUC_DEV uint32_t strip_block_scan(uint32_t v, uint32_t *smem /* >= kStripThreads
 // the scene's covered rectangle start at ~0 in shared memory; the warps
 // claim runs of kStripClaim items of its entries from a shared counter and
 // walk them with shared-memory reductions; every key the unit lowered is
-// then merged into vbuf (which k_init seeded) with one 64-bit min.
+// then merged into vbuf (which k_init seeded) with one 64-bit min and put
+// back to ~0 for the next unit.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kStripThreads, kStripBlocksPerSm) k_strip(const SceneDev *__restrict__ sc,
                                                             const uint64_t *__restrict__ sbase, int nsc,
@@ -1529,13 +1542,19 @@ __global__ void __launch_bounds__(kStripThreads, kStripBlocksPerSm) k_strip(cons
     __shared__ uint8_t s_nr[kStripUnit];            // its rows within the strip
     __shared__ uint32_t s_bkt[kWidthBuckets];       // entries per width bucket, then the bucket's first position
     __shared__ uint32_t s_scan[kStripThreads / 32 + 1];
+    __shared__ uint16_t s_first[kStripUnit * kStripMaxRows / 32];  // entry holding item 32k of the unit
     __shared__ uint32_t s_u, s_next;
     static_assert(2 * kStripThreads == kStripUnit && kStripMaxRows <= 255, "two entries per thread, rows in 8 bits");
+    static_assert(kStripMaxRows < 32 && kStripClaim % 32 == 0 && kStripUnit <= 65536,
+                  "one table slot per entry at most, claims start at a slot, entries in 16 bits");
     static_assert(offsetof(TriRec, bx0) == 48, "k_strip reads the bbox width from 8-byte word 6 of a record");
     const int tid = threadIdx.x, lane = tid & 31;
     const uint32_t nstrips = (uint32_t)sbase[nsc];
     const uint32_t nunits = strip_uoff[nstrips];
     const uint32_t keys_saddr = (uint32_t)__cvta_generic_to_shared(s_keys);
+    uint32_t key_bytes;  // the launch's dynamic shared memory
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(key_bytes));
+    for (uint32_t i = tid; i < key_bytes / 8; i += kStripThreads) s_keys[i] = ~0ull;
     for (;;) {
         if (tid == 0) {
             s_u = (uint32_t)atomicAdd(totals + 7, 1ull);
@@ -1612,7 +1631,10 @@ __global__ void __launch_bounds__(kStripThreads, kStripBlocksPerSm) k_strip(cons
         const uint32_t pre = strip_block_scan(n0 + n1, s_scan, &total);
         s_pref[2 * tid] = pre;
         s_pref[2 * tid + 1] = pre + n0;
-        for (uint32_t i = tid; i < area; i += kStripThreads) s_keys[i] = ~0ull;
+        // an entry has at most kStripMaxRows < 32 items, so at most one
+        // multiple of 32 falls in its range
+        if (n0 && ((pre + 31u) & ~31u) < pre + n0) s_first[(pre + 31u) >> 5] = (uint16_t)(2 * tid);
+        if (n1 && ((pre + n0 + 31u) & ~31u) < pre + n0 + n1) s_first[(pre + n0 + 31u) >> 5] = (uint16_t)(2 * tid + 1);
         __syncthreads();
         uint32_t cnt = 0;
         if (!err[si] && !empty) {  // a scene with a bad index draws nothing
@@ -1621,12 +1643,7 @@ __global__ void __launch_bounds__(kStripThreads, kStripBlocksPerSm) k_strip(cons
                 if (lane == 0) i0 = atomicAdd(&s_next, kStripClaim);
                 i0 = __shfl_sync(0xFFFFFFFFu, i0, 0);
                 if (i0 >= total) break;
-                int lo = 0, hi = nload;  // the entry of item i0: largest a with s_pref[a] <= i0
-                while (hi - lo > 1) {
-                    const int mid = (lo + hi) >> 1;
-                    if (s_pref[mid] <= i0) lo = mid; else hi = mid;
-                }
-                int a0 = lo;
+                int a0 = s_first[i0 >> 5];  // the entry of item i0 (a multiple of kStripClaim)
                 const uint32_t iend = min(total, i0 + kStripClaim);
                 // 32 consecutive items at a time: their entries are a run from
                 // a0 (every entry has at least one row)
@@ -1653,12 +1670,24 @@ __global__ void __launch_bounds__(kStripThreads, kStripBlocksPerSm) k_strip(cons
             }
         }
         __syncthreads();
-        // merge the keys this unit lowered, and its candidates
-        unsigned long long *dst = vbuf + s.pix_base;
-        for (uint32_t i = tid; i < area; i += kStripThreads) {
-            const unsigned long long k = s_keys[i];
-            const uint32_t ry = i / pitch, rx = i - ry * pitch;
-            if (k != ~0ull && rx < wc) atomicMin(dst + (uint64_t)(r0 + ry) * s.W + cx0 + rx, k);
+        // merge the keys this unit lowered (the padding column is never
+        // written) and put them back to ~0; key i is at row i / pitch, column
+        // i % pitch, stepped by kStripThreads without a division
+        if (area) {
+            const uint32_t qs = kStripThreads / pitch, rs = kStripThreads - qs * pitch;
+            uint32_t ry = tid / pitch, rx = tid - ry * pitch;
+            unsigned long long *drow = vbuf + s.pix_base + (uint64_t)(r0 + ry) * s.W + cx0;
+            for (uint32_t i = tid; i < area; i += kStripThreads) {
+                const unsigned long long k = s_keys[i];
+                if (k != ~0ull) {
+                    atomicMin(drow + rx, k);
+                    s_keys[i] = ~0ull;
+                }
+                rx += rs;
+                const uint32_t wrap = rx >= pitch ? 1u : 0u;
+                rx -= wrap * pitch;
+                drow += (uint64_t)(qs + wrap) * s.W;
+            }
         }
         const uint32_t wsum = warp_sum(cnt);
         if (lane == 0 && wsum) atomicAdd(&stats[si].candidates, (unsigned long long)wsum);
