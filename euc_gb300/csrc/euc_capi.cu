@@ -391,8 +391,10 @@ void prof_mark(euc_ctx *ctx, int stage, cudaEvent_t a, cudaEvent_t b) {
 
 template <class F>
 void launch_vertex(const SceneDev *sc, const uint64_t *vb, int s0, int s1, uint64_t blk0, uint64_t nblk, euc_ctx *ctx,
-                   cudaStream_t st) {
-    if (nblk) k_vertex<F><<<(unsigned)nblk, kBlock, 0, st>>>(sc, vb, s0, s1, blk0, (float4 *)ctx->clip.p, (float *)ctx->vdata.p);
+                   cudaStream_t st, const PrepArgs &prep) {
+    if (nblk)
+        k_vertex<F><<<(unsigned)nblk, kBlock, 0, st>>>(sc, vb, s0, s1, blk0, (float4 *)ctx->clip.p, (float *)ctx->vdata.p,
+                                                       prep);
 }
 
 // rbase: the device chunk bases of plan_chunks; nblk: an upper bound of the
@@ -428,14 +430,14 @@ void launch_resolve(const SceneDev *sc, const uint64_t *rbase, int s0, int s1, u
 }
 
 void dispatch_vertex(uint32_t shader, const SceneDev *sc, const uint64_t *vb, int s0, int s1, uint64_t blk0, uint64_t nblk,
-                     euc_ctx *ctx, cudaStream_t st) {
+                     euc_ctx *ctx, cudaStream_t st, const PrepArgs &prep) {
     switch (shader) {
-    case EUC_SHADER_FLAT: launch_vertex<FlatFn>(sc, vb, s0, s1, blk0, nblk, ctx, st); break;
-    case EUC_SHADER_VCOLOR: launch_vertex<VColorFn>(sc, vb, s0, s1, blk0, nblk, ctx, st); break;
-    case EUC_SHADER_GOURAUD: launch_vertex<GouraudFn>(sc, vb, s0, s1, blk0, nblk, ctx, st); break;
-    case EUC_SHADER_TEXTURED: launch_vertex<TexturedFn>(sc, vb, s0, s1, blk0, nblk, ctx, st); break;
-    case EUC_SHADER_PHONG: launch_vertex<PhongFn>(sc, vb, s0, s1, blk0, nblk, ctx, st); break;
-    case EUC_SHADER_SHADOW: launch_vertex<ShadowFn>(sc, vb, s0, s1, blk0, nblk, ctx, st); break;
+    case EUC_SHADER_FLAT: launch_vertex<FlatFn>(sc, vb, s0, s1, blk0, nblk, ctx, st, prep); break;
+    case EUC_SHADER_VCOLOR: launch_vertex<VColorFn>(sc, vb, s0, s1, blk0, nblk, ctx, st, prep); break;
+    case EUC_SHADER_GOURAUD: launch_vertex<GouraudFn>(sc, vb, s0, s1, blk0, nblk, ctx, st, prep); break;
+    case EUC_SHADER_TEXTURED: launch_vertex<TexturedFn>(sc, vb, s0, s1, blk0, nblk, ctx, st, prep); break;
+    case EUC_SHADER_PHONG: launch_vertex<PhongFn>(sc, vb, s0, s1, blk0, nblk, ctx, st, prep); break;
+    case EUC_SHADER_SHADOW: launch_vertex<ShadowFn>(sc, vb, s0, s1, blk0, nblk, ctx, st, prep); break;
     }
 }
 
@@ -597,7 +599,9 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
     const size_t off_gb = off_rb + pad_up(ns * sizeof(uint64_t), 16);
     const size_t off_sb = off_gb + pad_up(ns * sizeof(uint64_t), 16);
     const size_t off_cs = off_sb + pad_up((ns + 1) * sizeof(uint64_t), 16);
-    size_t off_u = off_cs + pad_up(nchunks * sizeof(uint32_t), 16);
+    // one scene needs no chunk -> scene table (the kernels read a null one as scene 0)
+    const bool one_scene = ns == 1;
+    size_t off_u = off_cs + (one_scene ? 0 : pad_up(nchunks * sizeof(uint32_t), 16));
     std::vector<size_t> uoff(ns);
     for (int i = 0; i < ns; ++i) {
         uoff[i] = off_u;
@@ -619,7 +623,7 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
     uint64_t *hvb = (uint64_t *)(h + off_vb), *hrb = (uint64_t *)(h + off_rb), *hgb = (uint64_t *)(h + off_gb);
     std::memcpy(h + off_sb, strip_first.data(), (ns + 1) * sizeof(uint64_t));
     uint32_t *hcs = (uint32_t *)(h + off_cs);
-    for (int i = 0; i < ns; ++i) {  // scene ranges of primitives are padded to whole setup chunks
+    for (int i = 0; i < ns && !one_scene; ++i) {  // scene ranges of primitives are padded to whole setup chunks
         const uint64_t c0 = plans[i].d.tri_base / kBlock, c1 = (i + 1 < ns ? plans[i + 1].d.tri_base : tri) / kBlock;
         for (uint64_t c = c0; c < c1; ++c) hcs[c] = (uint32_t)i;
     }
@@ -636,22 +640,36 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
     const SceneDev *dsc = (const SceneDev *)(dv + off_sc);
     const uint64_t *dvb = (const uint64_t *)(dv + off_vb), *drb = (const uint64_t *)(dv + off_rb),
                    *dgb = (const uint64_t *)(dv + off_gb), *dsb = (const uint64_t *)(dv + off_sb);
-    const uint32_t *dcs = (const uint32_t *)(dv + off_cs);
-    const uint64_t nprep = std::max<uint64_t>(std::max<uint64_t>((uint64_t)ns, nchunks), std::max<uint64_t>(nstrips, 2));
-    k_prep<<<(unsigned)((nprep + kBlock - 1) / kBlock), kBlock, 0, st>>>(
-        (int *)ctx->err.p, (SceneStats *)ctx->stats.p, (uint4 *)ctx->cov.p, ns, (uint2 *)ctx->chunk_sums.p, nchunks,
-        (uint32_t *)ctx->strip_cnt.p, (uint32_t *)ctx->strip_fill.p, (uint32_t)nstrips,
-        (unsigned long long *)ctx->totals.p);
-    // vertex stage, one launch per shader kind
+    const uint32_t *dcs = one_scene ? nullptr : (const uint32_t *)(dv + off_cs);
+    PrepArgs prep = {};
+    prep.err = (int *)ctx->err.p;
+    prep.stats = (SceneStats *)ctx->stats.p;
+    prep.cov = (uint4 *)ctx->cov.p;
+    prep.chunk_sums = (uint2 *)ctx->chunk_sums.p;
+    prep.strip_cnt = (uint32_t *)ctx->strip_cnt.p;
+    prep.strip_fill = (uint32_t *)ctx->strip_fill.p;
+    prep.totals = (unsigned long long *)ctx->totals.p;
+    prep.nchunks = nchunks;
+    prep.n = std::max<uint64_t>(std::max<uint64_t>((uint64_t)ns, nchunks), std::max<uint64_t>(nstrips, 2));
+    prep.nsc = (uint32_t)ns;
+    prep.nstrips = (uint32_t)nstrips;
+    // vertex stage, one launch per shader kind; the first also does the clears
     cudaEvent_t e0 = prof_event(ctx, st);
+    const PrepArgs no_prep = {};
+    bool prepped = false;
     for (int a = 0; a < ns;) {
         int b = a;
         while (b < ns && plans[b].d.shader == plans[a].d.shader) ++b;
         const uint64_t blk0 = plans[a].d.vtx_base / kBlock;
         const uint64_t blk1 = (b < ns ? plans[b].d.vtx_base : vtx_stage) / kBlock;
-        dispatch_vertex(plans[a].d.shader, dsc, dvb, a, b, blk0, blk1 - blk0, ctx, st);
+        dispatch_vertex(plans[a].d.shader, dsc, dvb, a, b, blk0, blk1 - blk0, ctx, st, prepped ? no_prep : prep);
+        prepped = prepped || blk1 > blk0;
         ctx->launches += blk1 > blk0;
         a = b;
+    }
+    if (!prepped) {
+        k_prep<<<(unsigned)((prep.n + kBlock - 1) / kBlock), kBlock, 0, st>>>(prep);
+        ctx->launches += 1;
     }
     // geometry stage, one launch per shader kind that has one
     for (int a = 0; a < ns && gin;) {
@@ -723,7 +741,7 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
                                        (const uint64_t *)ctx->live_rowoff.p, (unsigned long long *)ctx->totals.p,
                                        (const int *)ctx->err.p, (unsigned long long *)ctx->vbuf.p,
                                        (SceneStats *)ctx->stats.p, 0, nullptr, witems, probe);
-    ctx->launches += 5;
+    ctx->launches += 4;
     // ordered scenes: scan the per-pixel counts, size the fragment buffer
     // (one stream synchronisation), fill the lists in a second raster pass
     int first_ordered = ns;
@@ -1028,33 +1046,49 @@ void graph_free(euc_graph *g) {
 // ---------------------------------------------------------------------------
 // euc_render's recorded shapes.  A plain render is eight dependent stream
 // operations (the scene-table copy and seven launches), and for a small
-// scene their launch latencies, not the kernels, set the time per call.  So
+// scene their latencies, not the kernels, set the time per call.  So
 // euc_render records the launches of a scene shape as a CUDA graph the
 // second time it sees that shape, and from then on a call of the same shape
-// fills the scene table and uniforms into one of the shape's page-locked
-// staging slots, copies them to the shape's device staging and replays the
-// graph: one copy and one graph launch.  A shape is everything that decides
-// the launches and their arguments: the scene record without its buffer
-// pointers, the uniform size, the launch shape (euc_tuning), and the
-// context's scratch buffers (a render that moved them retires the shape's
-// graph).  Ordered-path scenes (which synchronise) and profiled renders stay
-// on the plain path.
+// fills the scene table and uniforms into the parameter of the graph's first
+// kernel (k_stage_param, which writes them to the shape's device staging)
+// and replays the graph: one parameter update and one graph launch.  The
+// staging travels with the launch, so the host keeps no ring of page-locked
+// slots and never waits for one; on GB300 the former copy of a page-locked
+// slot ahead of each replay took 32.5 us of device time per 640x480 sphere
+// frame, the parameter 28.7 us.  A shape is
+// everything that decides the launches and their arguments: the scene record
+// without its buffer pointers, the uniform size, the launch shape
+// (euc_tuning), and the context's scratch buffers (a render that moved them
+// retires the shape's graph).  Ordered-path scenes (which synchronise),
+// profiled renders and scenes whose staging exceeds the parameter stay on the
+// plain path.
 // ---------------------------------------------------------------------------
-constexpr int kShapeSlots = 4;     // staging slots of a recorded shape
 constexpr size_t kShapeCap = 512;  // recorded shapes of a context at most (least recently used go)
 constexpr size_t kSightCap = 4096; // shapes counted before the count starts over
+constexpr size_t kStageParamBytes = 1008;  // one scene's table, bases and uniforms (at most 240 + 64 + 512)
+
+struct alignas(16) StageParam {
+    uint32_t n, pad[3];                  // bytes of b to write (a multiple of 16)
+    unsigned char b[kStageParamBytes];  // the staging, laid out as run_batch reads it
+};
+
+// The first node of a recorded shape: writes its parameter's staging bytes
+// to the shape's device staging.
+__global__ void __launch_bounds__(64) k_stage_param(const __grid_constant__ StageParam p, unsigned char *__restrict__ dst) {
+    for (uint32_t i = threadIdx.x * 16u; i < p.n; i += blockDim.x * 16u)
+        *reinterpret_cast<uint4 *>(dst + i) = *reinterpret_cast<const uint4 *>(p.b + i);
+}
 
 struct ShapeGraph {
     std::vector<unsigned char> key;
     void *scratch[kScratchBufs] = {};
-    unsigned char *host = nullptr;  // kShapeSlots staging slots of `stride` bytes
+    StageParam param;               // the next replay's staging
     void *dev = nullptr;            // the staging the graph's kernels read
-    size_t need = 0, stride = 0;
+    size_t need = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    cudaEvent_t slot_done[kShapeSlots] = {};
-    bool slot_pending[kShapeSlots] = {};
-    int next = 0;
+    cudaGraphNode_t stage_node = nullptr;  // the k_stage_param node
+    cudaKernelNodeParams stage_kp = {};
     cudaEvent_t done = nullptr;  // after the last replay
     bool launched = false;
     uint64_t launches = 0, last_use = 0;
@@ -1064,12 +1098,9 @@ namespace {
 
 void shape_free(ShapeGraph *g) {
     if (g->launched) cudaEventSynchronize(g->done);
-    for (int k = 0; k < kShapeSlots; ++k)
-        if (g->slot_done[k]) cudaEventDestroy(g->slot_done[k]);
     if (g->done) cudaEventDestroy(g->done);
     if (g->exec) cudaGraphExecDestroy(g->exec);
     if (g->graph) cudaGraphDestroy(g->graph);
-    if (g->host) cudaFreeHost(g->host);
     if (g->dev) cudaFree(g->dev);
     delete g;
 }
@@ -1099,34 +1130,38 @@ ShapeGraph *shape_record(euc_ctx *ctx, const euc_scene &s, std::vector<unsigned 
     StageOverride so;
     so.dry = true;
     if (run_batch(ctx, &s, 1, nullptr, &so)) return nullptr;  // validates, sizes the scratch
+    if (so.need > kStageParamBytes) return nullptr;  // too large for the parameter: plain path
     ShapeGraph *g = new (std::nothrow) ShapeGraph();
     if (!g) return nullptr;
     g->key = std::move(key);
-    g->need = std::max<size_t>(so.need, 256);
-    g->stride = pad_up(g->need, 256);
-    bool ok = cudaMallocHost((void **)&g->host, g->stride * kShapeSlots) == cudaSuccess &&
-              cudaMalloc(&g->dev, g->need) == cudaSuccess &&
+    g->need = so.need;
+    g->param.n = (uint32_t)so.need;
+    bool ok = cudaMalloc(&g->dev, std::max<size_t>(g->need, 16)) == cudaSuccess &&
               cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming) == cudaSuccess;
-    for (int k = 0; ok && k < kShapeSlots; ++k)
-        ok = cudaEventCreateWithFlags(&g->slot_done[k], cudaEventDisableTiming) == cudaSuccess;
     cudaStream_t cs = nullptr;
     ok = ok && cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess;
     if (ok && cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
         so.dry = false;
         so.no_copy = true;
-        so.host = g->host;
+        so.host = g->param.b;
         so.dev = g->dev;
         so.need = g->need;
         ctx->capturing = true;
         const uint64_t l0 = ctx->launches;
+        k_stage_param<<<1, 64, 0, cs>>>(g->param, (unsigned char *)g->dev);
         const int rc = run_batch(ctx, &s, 1, cs, &so);
-        g->launches = ctx->launches - l0;
+        g->launches = ctx->launches - l0 + 1;
         ctx->launches = l0;
         ctx->capturing = false;
         cudaGraph_t graph = nullptr;
         const cudaError_t ec = cudaStreamEndCapture(cs, &graph);
         g->graph = graph;
+        // the staging node is the graph's only root
+        size_t nroot = 1;
         ok = rc == EUC_OK && ec == cudaSuccess && graph &&
+             cudaGraphGetRootNodes(graph, &g->stage_node, &nroot) == cudaSuccess && nroot == 1 &&
+             cudaGraphKernelNodeGetParams(g->stage_node, &g->stage_kp) == cudaSuccess &&
+             g->stage_kp.func == (void *)k_stage_param &&
              cudaGraphInstantiate(&g->exec, g->graph, 0) == cudaSuccess;
     } else {
         ok = false;
@@ -1177,23 +1212,19 @@ int render_one(euc_ctx *ctx, const euc_scene &s, cudaStream_t st) {
         ctx->shapes.push_back(g);
     }
     g->last_use = ++ctx->shape_clock;
-    const int k = g->next;
-    g->next = (k + 1) % kShapeSlots;
-    if (g->slot_pending[k]) {  // the slot's previous copy has been read
-        CUDA_TRY(cudaEventSynchronize(g->slot_done[k]));
-        g->slot_pending[k] = false;
-    }
-    unsigned char *slot = g->host + (size_t)k * g->stride;
     StageOverride so;
     so.fill = true;
-    so.host = slot;
+    so.host = g->param.b;
     so.dev = g->dev;
     so.need = g->need;
     if (int rc = run_batch(ctx, &s, 1, st, &so)) return rc;
+    // the parameter is copied here; replays already enqueued keep theirs
+    void *args[2] = {&g->param, &g->dev};
+    cudaKernelNodeParams kp = g->stage_kp;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    CUDA_TRY(cudaGraphExecKernelNodeSetParams(g->exec, g->stage_node, &kp));
     if (g->launched) CUDA_TRY(cudaStreamWaitEvent(st, g->done, 0));  // a replay on another stream has finished
-    CUDA_TRY(cudaMemcpyAsync(g->dev, slot, g->need, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaEventRecord(g->slot_done[k], st));
-    g->slot_pending[k] = true;
     CUDA_TRY(cudaGraphLaunch(g->exec, st));
     CUDA_TRY(cudaEventRecord(g->done, st));
     g->launched = true;
@@ -1720,7 +1751,7 @@ void na_vertex_resolve(bool vertex, const SceneDev *sc, const uint64_t *base, ui
     if (!nblk) return;
     if (vertex)
         k_vertex<F><<<(unsigned)nblk, kBlock, 0, st>>>(sc, base, 0, 1, 0, (float4 *)(a + kNaOffClip),
-                                                       (float *)(a + kNaOffVdata));
+                                                       (float *)(a + kNaOffVdata), PrepArgs{});
     else
         k_resolve<F><<<chunk_grid(nblk, t_na_nsm), kBlock, 0, st>>>(
             sc, base, 0, 1, chunk_group(nblk, t_na_nsm), (const TriRec *)(a + kNaOffRecs),
@@ -1798,9 +1829,16 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
     k_na_stage<<<1, 128, 0, st>>>(stage, a, (uint32_t)off_b, (uint32_t)off_u, (uint32_t)p.usize);
     const SceneDev *dsc = (const SceneDev *)a;
     const uint64_t *zero_base = (const uint64_t *)(a + off_b);  // every base is 0 for a single scene
-    k_prep<<<(unsigned)((tri / kBlock + kBlock - 1) / kBlock), kBlock, 0, st>>>(
-        (int *)(a + kNaOffErr), (SceneStats *)(a + kNaOffStats), (uint4 *)(a + kNaOffCov), 1,
-        (uint2 *)(a + kNaOffChunks), tri / kBlock, nullptr, nullptr, 0, (unsigned long long *)(a + kNaOffTotals));
+    PrepArgs prep = {};
+    prep.err = (int *)(a + kNaOffErr);
+    prep.stats = (SceneStats *)(a + kNaOffStats);
+    prep.cov = (uint4 *)(a + kNaOffCov);
+    prep.chunk_sums = (uint2 *)(a + kNaOffChunks);
+    prep.totals = (unsigned long long *)(a + kNaOffTotals);
+    prep.nchunks = tri / kBlock;
+    prep.n = std::max<uint64_t>(prep.nchunks, 2);
+    prep.nsc = 1;
+    k_prep<<<(unsigned)((prep.n + kBlock - 1) / kBlock), kBlock, 0, st>>>(prep);
     t_na_nsm = nsm;
     na_dispatch(true, d.shader, dsc, zero_base, vtx / kBlock, a, st);
     k_setup<<<(unsigned)(tri / kBlock), kBlock, 0, st>>>(dsc, nullptr, (const float4 *)(a + kNaOffClip),

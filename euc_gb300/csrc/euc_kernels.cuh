@@ -9,7 +9,8 @@
 //                 reverse, weight matrix, screen bbox, per-pixel weight deltas,
 //                 vertices by y, z-clip class (triangles.rs:55-199)
 //   k_prep        per batch: clears the error, statistics, covered-rectangle
-//                 and setup-sum entries
+//                 and setup-sum entries (done by the first k_vertex launch
+//                 when the batch has one)
 //   k_scan_plan   exclusive scan of per-primitive row counts, compaction of the
 //                 primitives that cover at least one row; one more block
 //                 plans the init / resolve chunks of every scene
@@ -250,12 +251,48 @@ EUC_DEV T block_excl_scan(T v, T *smem /* >= kBlock/32 + 1 */, T *total) {
 }
 
 // ---------------------------------------------------------------------------
+// The per-batch clears before k_setup: each scene's error, statistics and
+// covered rectangle, the setup-chunk sums, the strip counts and the strip
+// path's counters (totals[6]: entries taken, totals[7]: k_strip's work
+// counter).  Entry i of the n = max(scenes, chunks, strips, 2) covers index i
+// of each.  The first vertex launch of a batch does them (nothing it reads or
+// writes is cleared), which saves a launch; k_prep does them when a batch has
+// no vertex launch, and on the no-allocation path.
+// ---------------------------------------------------------------------------
+struct PrepArgs {
+    int *err;
+    SceneStats *stats;
+    uint4 *cov;
+    uint2 *chunk_sums;
+    uint32_t *strip_cnt, *strip_fill;
+    unsigned long long *totals;
+    uint64_t nchunks, n;  // n = 0: nothing to clear
+    uint32_t nsc, nstrips;
+};
+
+EUC_DEV void prep_clear(const PrepArgs &a, uint64_t i) {
+    if (i < a.nsc) {
+        a.err[i] = 0;
+        a.stats[i] = SceneStats{};
+        a.cov[i] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+    }
+    if (i < a.nchunks) a.chunk_sums[i] = make_uint2(0u, 0u);
+    if (i < a.nstrips) {
+        a.strip_cnt[i] = 0;
+        a.strip_fill[i] = 0;
+    }
+    if (i < 2) a.totals[6 + i] = 0;
+}
+
+// ---------------------------------------------------------------------------
 // k_vertex
 // ---------------------------------------------------------------------------
 template <class F>
 __global__ void __launch_bounds__(kBlock) k_vertex(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ vtx_base,
                                                    int s_begin, int s_end, uint64_t blk_begin, float4 *__restrict__ clip,
-                                                   float *__restrict__ vdata) {
+                                                   float *__restrict__ vdata, const PrepArgs prep) {
+    for (uint64_t i = (uint64_t)blockIdx.x * kBlock + threadIdx.x; i < prep.n; i += (uint64_t)gridDim.x * kBlock)
+        prep_clear(prep, i);
     __shared__ int s_scene;
     const uint64_t pos = (blk_begin + blockIdx.x) * (uint64_t)kBlock;
     if (threadIdx.x == 0) s_scene = s_begin + find_scene(vtx_base + s_begin, s_end - s_begin, pos);
@@ -547,7 +584,7 @@ constexpr uint32_t kStripMaxRows = 16;        // rows of a strip at most
 constexpr size_t kStripKeyBytes = 96 * 1024;  // a strip's keys in shared memory at most
 constexpr uint32_t kRowsBinned = 0x80000000u; // rows[t]: the primitive went to the strips
 constexpr uint32_t kStripUnit = 1024;         // entries of one strip a k_strip block takes at once at most
-constexpr uint32_t kStripClaim = 64;          // items a k_strip warp claims at a time
+constexpr uint32_t kStripClaim = 32;          // items a k_strip warp claims at a time
 constexpr uint64_t kStripOverdraw = 4;        // fragments per covered pixel that route a scene to the strips ...
 constexpr uint64_t kStripTriFrags = 16;       // ... when its triangles make this many fragments each on average
 constexpr uint64_t kStripMinPixels = 64;      // target pixels per primitive above which a scene stays off them
@@ -1931,27 +1968,10 @@ __global__ void __launch_bounds__(kBlock) k_scan_plan(const uint32_t *__restrict
     else scan_block(rows, chunk_sums, ntri, live_tri, live_rowoff, totals, nscan);
 }
 
-// Per batch, before k_setup: no errors, zero statistics, empty covered
-// rectangles, zero setup-chunk sums, zero strip counts and fill cursors, and
-// the strip path's counters (totals[6]: entries taken, totals[7]: k_strip's
-// work counter).
-__global__ void __launch_bounds__(kBlock) k_prep(int *__restrict__ err, SceneStats *__restrict__ stats,
-                                                 uint4 *__restrict__ cov, int nsc, uint2 *__restrict__ chunk_sums,
-                                                 uint64_t nchunks, uint32_t *__restrict__ strip_cnt,
-                                                 uint32_t *__restrict__ strip_fill, uint32_t nstrips,
-                                                 unsigned long long *__restrict__ totals) {
+// The clears of prep_clear as a launch of their own (n threads).
+__global__ void __launch_bounds__(kBlock) k_prep(const PrepArgs prep) {
     const uint64_t i = (uint64_t)blockIdx.x * kBlock + threadIdx.x;
-    if (i < (uint64_t)nsc) {
-        err[i] = 0;
-        stats[i] = SceneStats{};
-        cov[i] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
-    }
-    if (i < nchunks) chunk_sums[i] = make_uint2(0u, 0u);
-    if (i < nstrips) {
-        strip_cnt[i] = 0;
-        strip_fill[i] = 0;
-    }
-    if (i < 2) totals[6 + i] = 0;
+    if (i < prep.n) prep_clear(prep, i);
 }
 
 // One warp's job list in k_resolve: its 32 pixels' winners and positions,
