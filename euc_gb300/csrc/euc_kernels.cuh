@@ -2023,43 +2023,46 @@ EUC_DEV void resolve_direct_chunk(const SceneDev &s, const uint4 &cv, uint64_t l
     }
 }
 
-// One 256-pixel chunk `lb` of scene `s`; every thread of the block calls it.
-template <class F>
-EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, const TriRec *__restrict__ recs,
-                           const float *__restrict__ vdata, const unsigned long long *__restrict__ vbuf,
-                           ResolveSmem<F> &sm) {
+// This thread's pixel in chunk lb of a scene's covered rectangle (which is
+// not empty, or the scene would have no chunks) and the first row of its band.
+EUC_DEV bool chunk_pixel(const SceneDev &s, const uint4 &cv, uint64_t lb, bool quads, uint32_t &x, uint32_t &y,
+                         uint32_t &lo) {
     const int tid = threadIdx.x, lane = tid & 31;
-    // 1. this thread's pixel: chunk lb of the covered rectangle (it is not
-    // empty, or the scene would have no chunks)
-    uint32_t x = 0, y = 0, lo = 0;
-    bool inside;
-    const bool quads = resolve_by_quads(s);
+    x = y = lo = 0;
     if (quads) {  // warp = 16x2 pixels on whole 2x2 cells of the band-relative grid
         const uint32_t ppb = (s.gr + 1) >> 1;
         const uint32_t p0 = pair_of_row(cv.y, s.gr), a0 = cv.x >> 4;
         const uint32_t cols = ((~cv.z - 1) >> 4) - a0 + 1;
         const uint64_t npairs = pair_of_row(~cv.w - 1, s.gr) - p0 + 1;
         const uint64_t w = lb * (kBlock / 32) + (tid >> 5);
-        inside = w < npairs * cols;
-        if (inside) {
-            const uint32_t p = p0 + (uint32_t)(w / cols), a = a0 + (uint32_t)(w % cols);
-            const uint32_t b = p / ppb, k = p % ppb;
-            lo = b * s.gr;
-            x = a * 16 + (lane & 15);
-            y = lo + 2 * k + (lane >> 4);
-            inside = x < s.W && y < min(lo + s.gr, s.H) && covered(cv, x, y);
-        }
-    } else {
-        const uint32_t rw = ~cv.z - cv.x;
-        const uint32_t i = (uint32_t)lb * kBlock + tid;  // pixel indices fit 32 bits (plan_scene)
-        inside = i < (uint32_t)rect_area(cv);
-        if (inside) {
-            const uint32_t ry = i / rw;
-            y = cv.y + ry;
-            x = cv.x + (i - ry * rw);
-            lo = (y / s.gr) * s.gr;
-        }
+        if (w >= npairs * cols) return false;
+        const uint32_t p = p0 + (uint32_t)(w / cols), a = a0 + (uint32_t)(w % cols);
+        const uint32_t b = p / ppb, k = p % ppb;
+        lo = b * s.gr;
+        x = a * 16 + (lane & 15);
+        y = lo + 2 * k + (lane >> 4);
+        return x < s.W && y < min(lo + s.gr, s.H) && covered(cv, x, y);
     }
+    const uint32_t rw = ~cv.z - cv.x;
+    const uint32_t i = (uint32_t)lb * kBlock + tid;  // pixel indices fit 32 bits (plan_scene)
+    if (i >= (uint32_t)rect_area(cv)) return false;
+    const uint32_t ry = i / rw;
+    y = cv.y + ry;
+    x = cv.x + (i - ry * rw);
+    lo = (y / s.gr) * s.gr;
+    return true;
+}
+
+// One 256-pixel chunk `lb` of scene `s`; every thread of the block calls it.
+template <class F>
+EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, const TriRec *__restrict__ recs,
+                           const float *__restrict__ vdata, const unsigned long long *__restrict__ vbuf,
+                           ResolveSmem<F> &sm) {
+    const int lane = threadIdx.x & 31;
+    // 1. this thread's pixel
+    uint32_t x, y, lo;
+    const bool quads = resolve_by_quads(s);
+    const bool inside = chunk_pixel(s, cv, lb, quads, x, y, lo);
     uint32_t t = 0xFFFFFFFFu;
     float z = 0.0f;
     const bool win = inside && decode_key(s, vbuf[s.pix_base + (uint64_t)y * s.W + x], t, z);
@@ -2179,7 +2182,16 @@ __global__ void __launch_bounds__(kBlock, 4) k_resolve(const SceneDev *__restric
             if (resolve_direct(s)) {  // uniform: one scene per chunk
                 resolve_direct_chunk<F>(s, cov[s_begin + si], c - base[si], recs, vdata, vbuf);
             } else {
-                resolve_chunk<F>(s, cov[s_begin + si], c - base[si], recs, vdata, vbuf, sm);
+                const uint4 cv = cov[s_begin + si];
+                // the keys of this block's next chunk in the same scene start
+                // on their way to L2 (the keys of a large batch outgrow it)
+                const uint64_t nc = c + 1 < c0 + group ? c + 1 : c_begin + (g + gridDim.x) * group;
+                if (nc < base[si + 1]) {
+                    uint32_t px, py, plo;
+                    if (chunk_pixel(s, cv, nc - base[si], resolve_by_quads(s), px, py, plo))
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(vbuf + s.pix_base + (uint64_t)py * s.W + px));
+                }
+                resolve_chunk<F>(s, cv, c - base[si], recs, vdata, vbuf, sm);
                 __syncwarp();  // the next chunk reuses the warp's shared memory
             }
         }
