@@ -61,6 +61,18 @@ EUC_DEV void normalize3(const float *a, float *out) {
     out[2] = a[2] / len;
 }
 
+// normalize3 with the hardware reciprocal square root: for lighting terms
+// only, whose result is a colour quantised to 8 bits.  Its relative error
+// (about 2^-22) moves a colour channel by far less than one step, so the
+// quantised colour stays within the +-1 per channel that colour parity
+// allows; coordinates that pick texels or shadow-map depths stay exact.
+EUC_DEV void normalize3_light(const float *a, float *out) {
+    const float r = rsqrtf(dot3(a, a));
+    out[0] = a[0] * r;
+    out[1] = a[1] * r;
+    out[2] = a[2] * r;
+}
+
 // ---------------------------------------------------------------------------
 // Samplers: sampler/mod.rs:100-179 (wraps), linear.rs:30-66, nearest.rs:27-33
 // ---------------------------------------------------------------------------
@@ -247,13 +259,14 @@ struct PhongFn {  // examples/teapot.rs:69-141 with a surface texture
     }
     static EUC_DEV void fragment(const U &u, const float *vd, float *f) {
         float n[3], cam_dir[3], light_dir[3], t[3];
-        normalize3(vd + 3, n);
+        // lighting terms: hardware reciprocal square root and power (see normalize3_light)
+        normalize3_light(vd + 3, n);
 #pragma unroll
         for (int i = 0; i < 3; ++i) t[i] = u.cam_pos[i] - vd[i];
-        normalize3(t, cam_dir);
+        normalize3_light(t, cam_dir);
 #pragma unroll
         for (int i = 0; i < 3; ++i) t[i] = vd[i] - u.light_pos[i];
-        normalize3(t, light_dir);
+        normalize3_light(t, light_dir);
         float surf[4];
         if (u.tex.data) {
             const Texel tx = sample2d(u.tex, vd[9], vd[10]);
@@ -269,7 +282,7 @@ struct PhongFn {  // examples/teapot.rs:69-141 with a surface texture
         const float dd = d + d;
         const float r[3] = {nl[0] - n[0] * dd, nl[1] - n[1] * dd, nl[2] - n[2] * dd};
         const float nc[3] = {-cam_dir[0], -cam_dir[1], -cam_dir[2]};
-        const float specular = powf(rmax(dot3(r, nc), 0.0f), 30.0f) * 3.0f;
+        const float specular = __powf(rmax(dot3(r, nc), 0.0f), 30.0f) * 3.0f;
         bool in_light = true;
         if (u.shadow.data) {
             const float su = (vd[6] * 1.0f) * 0.5f + 0.5f;
