@@ -80,6 +80,17 @@ struct Texel {
     float c[4];
 };
 
+// (float)b / 255.0f for every byte b, evaluated by the compiler (correctly
+// rounded, as the division on the device is): an RGBA8 texel's channels are
+// looked up here instead of divided, four divisions per texel saved.
+struct ByteOver255 {
+    float v[256];
+    constexpr ByteOver255() : v() {
+        for (int i = 0; i < 256; ++i) v[i] = (float)i / 255.0f;
+    }
+};
+__device__ const ByteOver255 g_byte_over_255 = ByteOver255();
+
 EUC_DEV Texel read_texel(const euc_sampler &s, uint32_t x, uint32_t y) {
     const uint32_t pitch = s.pitch ? s.pitch : s.width * 4u;
     const uint8_t *p = reinterpret_cast<const uint8_t *>(s.data) + (uint64_t)y * pitch + (uint64_t)x * 4u;
@@ -88,9 +99,18 @@ EUC_DEV Texel read_texel(const euc_sampler &s, uint32_t x, uint32_t y) {
         float f = __ldg(reinterpret_cast<const float *>(p));
         t.c[0] = t.c[1] = t.c[2] = t.c[3] = f;
     } else {
+        // (u8 as f32) / texel_div (texture.rs:84-94); texel_div is 1 or 255
         uint32_t w = __ldg(reinterpret_cast<const unsigned int *>(p));
+        if (s.texel_div == 255.0f) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) t.c[i] = (float)((w >> (8 * i)) & 0xFFu) / s.texel_div;  // texture.rs:84-94
+            for (int i = 0; i < 4; ++i) t.c[i] = __ldg(g_byte_over_255.v + ((w >> (8 * i)) & 0xFFu));
+        } else if (s.texel_div == 1.0f) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) t.c[i] = (float)((w >> (8 * i)) & 0xFFu);
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) t.c[i] = (float)((w >> (8 * i)) & 0xFFu) / s.texel_div;
+        }
     }
     return t;
 }
