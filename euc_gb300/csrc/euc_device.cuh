@@ -38,8 +38,16 @@ EUC_DEV uint32_t sat_u8(float v) {
 
 EUC_DEV float rfract(float v) { return v - truncf(v); }  // f32::fract
 
-EUC_DEV float rem_euclid(float x, float m) {  // f32::rem_euclid
-    float r = fmodf(x, m);
+// fmodf(x, m) for m = 1 or 2 (the wraps' moduli): x - m * trunc(x / m) is
+// exact there (the quotient by a power of two, its truncation and the product
+// are exact, and the difference, a multiple of x's ulp below 2 in magnitude,
+// is representable), and fmodf's result has the sign of x.
+__host__ __device__ inline float fmod_1_or_2(float x, float m) {
+    return copysignf(x - m * truncf(x * (m == 1.0f ? 1.0f : 0.5f)), x);
+}
+
+EUC_DEV float rem_euclid(float x, float m) {  // f32::rem_euclid, m = 1 or 2
+    float r = fmod_1_or_2(x, m);
     return r < 0.0f ? r + fabsf(m) : r;
 }
 
