@@ -54,6 +54,7 @@ struct euc_ctx {
     // strip path: per-strip entry counts, fill cursors, list offsets, unit
     // offsets, the entry lists and the strip of each unit
     DevBuf strip_cnt, strip_fill, strip_off, strip_uoff, entries, unit_strip;
+    DevBuf bbox;  // strip path: each primitive's bbox (16 B), the binning's only read of it
     int raster_blocks = 0;  // resident k_raster blocks per SM
     bool pageable = false;  // kernels may access pageable host memory (cudaDevAttrPageableMemoryAccess)
     euc_tuning tune{};      // launch-shape overrides (0 = default)
@@ -590,6 +591,7 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
         if ((rc = grow(ctx->strip_uoff, (nstrips + 1) * sizeof(uint32_t)))) return rc;
         if ((rc = grow(ctx->entries, entry_cap * sizeof(uint2)))) return rc;
         if ((rc = grow(ctx->unit_strip, (nstrips + entry_cap / kStripUnit + 1) * sizeof(uint32_t)))) return rc;
+        if ((rc = grow(ctx->bbox, tri * sizeof(uint4)))) return rc;
     }
     // staging: scene table | vtx bases | resolve bases | geometry bases |
     // first strip of each scene | scene of each setup chunk | uniforms
@@ -687,12 +689,13 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
                                                    (TriRec *)ctx->recs.p, (uint32_t *)ctx->rows.p,
                                                    (uint2 *)ctx->chunk_sums.p, (int *)ctx->err.p,
                                                    (SceneStats *)ctx->stats.p, (uint4 *)ctx->cov.p,
-                                                   (const uint8_t *)ctx->galive.p);
+                                                   (const uint8_t *)ctx->galive.p,
+                                                   nstrips ? (uint4 *)ctx->bbox.p : nullptr);
     // binning blocks stride the setup chunks
     const unsigned bin_grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(nchunks, (uint64_t)ctx->nsm * 8));
     if (nstrips) {  // the strip path's routing and counts
         k_bin_count<<<bin_grid, kBlock, 0, st>>>(
-            dsc, dcs, nchunks, (uint32_t *)ctx->rows.p, (const TriRec *)ctx->recs.p, (const uint4 *)ctx->cov.p,
+            dsc, dcs, nchunks, (uint32_t *)ctx->rows.p, (const uint4 *)ctx->bbox.p, (const uint4 *)ctx->cov.p,
             (const SceneStats *)ctx->stats.p, (uint2 *)ctx->chunk_sums.p, (uint32_t *)ctx->strip_cnt.p,
             (unsigned long long *)ctx->totals.p + 6, entry_cap, strip_mode);
         ctx->launches += 1;
@@ -713,7 +716,7 @@ int run_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, cudaStream_t st, 
         chunk_group(ichunks, ctx->nsm, tu.chunk_group, tu.chunk_blocks_per_sm));
     cudaEvent_t e4 = prof_event(ctx, st);
     if (nstrips) {  // the strip lists, then the strips (after k_init, before the item queue)
-        k_bin<<<bin_grid, kBlock, 0, st>>>(dsc, dcs, nchunks, (const uint32_t *)ctx->rows.p, (const TriRec *)ctx->recs.p,
+        k_bin<<<bin_grid, kBlock, 0, st>>>(dsc, dcs, nchunks, (const uint32_t *)ctx->rows.p, (const uint4 *)ctx->bbox.p,
                                            (const uint4 *)ctx->cov.p, (const SceneStats *)ctx->stats.p,
                                            (const uint32_t *)ctx->strip_off.p, (uint32_t *)ctx->strip_fill.p,
                                            (uint2 *)ctx->entries.p, strip_mode);
@@ -858,7 +861,7 @@ int euc_ctx_destroy(euc_ctx *ctx) {
     DevBuf *bufs[] = {&ctx->clip, &ctx->vdata, &ctx->recs, &ctx->rows, &ctx->chunk_sums, &ctx->live_tri, &ctx->live_rowoff,
                       &ctx->totals, &ctx->vbuf, &ctx->err, &ctx->stats, &ctx->cov, &ctx->obsum, &ctx->frags,
                       &ctx->plan, &ctx->galive, &ctx->h_arena, &ctx->h_tex[0], &ctx->strip_cnt, &ctx->strip_fill,
-                      &ctx->strip_off, &ctx->strip_uoff, &ctx->entries, &ctx->unit_strip};
+                      &ctx->strip_off, &ctx->strip_uoff, &ctx->entries, &ctx->unit_strip, &ctx->bbox};
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (ctx->h_pinned.p) cudaFreeHost(ctx->h_pinned.p);
@@ -1009,6 +1012,9 @@ int euc_render_batch(euc_ctx *ctx, const euc_scene *scenes, size_t n, void *stre
 
 }  // extern "C"
 
+// The scratch buffers a recorded batch reads and writes (scratch_ptrs).
+constexpr int kScratchBufs = 21;
+
 struct euc_graph {
     euc_ctx *ctx = nullptr;
     void *host = nullptr;  // staging owned by the graph: read by every replay
@@ -1017,19 +1023,19 @@ struct euc_graph {
     cudaGraphExec_t exec = nullptr;
     int nscenes = 0;
     uint64_t launches = 0;   // kernels in the recorded batch
-    void *scratch[20] = {};  // the context's scratch pointers the graph was recorded with
+    void *scratch[kScratchBufs] = {};  // the context's scratch pointers the graph was recorded with
 };
 
 namespace {
 
 // The scratch buffers a recorded batch reads and writes.  A later render that
 // grows one of them moves it, and the graph may then no longer be launched.
-constexpr int kScratchBufs = 20;
 void scratch_ptrs(const euc_ctx *c, void *out[kScratchBufs]) {
     const DevBuf *b[kScratchBufs] = {&c->clip,       &c->vdata,      &c->recs,      &c->rows,       &c->chunk_sums,
                                      &c->live_tri,   &c->live_rowoff, &c->totals,   &c->vbuf,       &c->err,
                                      &c->stats,      &c->cov,        &c->plan,      &c->galive,     &c->strip_cnt,
-                                     &c->strip_fill, &c->strip_off,  &c->strip_uoff, &c->entries,  &c->unit_strip};
+                                     &c->strip_fill, &c->strip_off,  &c->strip_uoff, &c->entries,  &c->unit_strip,
+                                     &c->bbox};
     for (int i = 0; i < kScratchBufs; ++i) out[i] = b[i]->p;
 }
 
@@ -1845,7 +1851,7 @@ extern "C" int euc_render_noalloc(const euc_pipeline_desc *desc, const void *uni
                                                           (TriRec *)(a + kNaOffRecs), (uint32_t *)(a + kNaOffRows),
                                                           (uint2 *)(a + kNaOffChunks), (int *)(a + kNaOffErr),
                                                           (SceneStats *)(a + kNaOffStats), (uint4 *)(a + kNaOffCov),
-                                                          nullptr);
+                                                          nullptr, nullptr);
     uint64_t *const ibase = (uint64_t *)(a + kNaOffPlan), *const rbase = ibase + 2;
     const uint32_t nscan = (uint32_t)((tri + kScanBlock - 1) / kScanBlock);
     k_scan_plan<<<nscan + 1, kBlock, 0, st>>>((const uint32_t *)(a + kNaOffRows), (const uint2 *)(a + kNaOffChunks),

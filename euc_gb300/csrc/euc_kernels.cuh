@@ -613,14 +613,17 @@ __host__ __device__ inline uint32_t width_bucket(uint32_t w) {
 // k_setup: triangles.rs:55-199, once per primitive (euc repeats it per band;
 // only the bbox clamp depends on the band and that is applied per row).
 // Block b sets up primitives [b * kBlock, (b + 1) * kBlock), all of scene
-// chunk_scene[b] (null: scene 0); chunk_sums must be zero at launch.
+// chunk_scene[b] (null: scene 0); chunk_sums must be zero at launch.  bbox
+// (null when the batch has no strips) receives the bbox of every triangle
+// with rows: the binning reads those 16 bytes instead of the record's line.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ sc,
                                                   const uint32_t *__restrict__ chunk_scene,
                                                   const float4 *__restrict__ clip, TriRec *__restrict__ recs,
                                                   uint32_t *__restrict__ rows, uint2 *__restrict__ chunk_sums,
                                                   int *__restrict__ err, SceneStats *__restrict__ stats,
-                                                  uint4 *__restrict__ cov, const uint8_t *__restrict__ galive) {
+                                                  uint4 *__restrict__ cov, const uint8_t *__restrict__ galive,
+                                                  uint4 *__restrict__ bbox) {
     // a warp's 32 records, staged so that they leave as 512-byte stores;
     // 16-byte word k of lane l's record sits at l * 8 + (k ^ (l & 7)), which
     // keeps both the staging and the copy-out at the minimum four wavefronts
@@ -812,6 +815,7 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
 #pragma unroll
                     for (int k = 0; k < 8; ++k) stage[lane * 8 + (k ^ (lane & 7))] = src[k];
                     staged = true;
+                    if (bbox) bbox[t] = make_uint4(bx0, bx1, by0, by1);  // the binning's copy
                     cx0 = bx0;
                     cx1 = bx1;
                     cy0 = by0;
@@ -1351,7 +1355,7 @@ EUC_DEV bool strip_routed(const SceneDev &s, const SceneStats &st, const uint4 &
 
 __global__ void __launch_bounds__(kBlock) k_bin_count(const SceneDev *__restrict__ sc,
                                                       const uint32_t *__restrict__ chunk_scene, uint64_t nchunks,
-                                                      uint32_t *__restrict__ rows, const TriRec *__restrict__ recs,
+                                                      uint32_t *__restrict__ rows, const uint4 *__restrict__ bbox,
                                                       const uint4 *__restrict__ cov,
                                                       const SceneStats *__restrict__ stats,
                                                       uint2 *__restrict__ chunk_sums, uint32_t *__restrict__ strip_cnt,
@@ -1370,7 +1374,7 @@ __global__ void __launch_bounds__(kBlock) k_bin_count(const SceneDev *__restrict
         const uint32_t nr = rows[t];
         uint32_t q0 = 0, nst = 0;
         if (nr) {
-            const uint4 w3 = __ldg(reinterpret_cast<const uint4 *>(recs + t) + 3);  // bx0, bx1, by0, by1
+            const uint4 w3 = __ldg(bbox + t);  // bx0, bx1, by0, by1
             q0 = w3.z / s.strip_h;
             nst = (w3.w - 1) / s.strip_h - q0 + 1;
         }
@@ -1409,7 +1413,7 @@ __global__ void __launch_bounds__(kBlock) k_bin_count(const SceneDev *__restrict
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kBlock) k_bin(const SceneDev *__restrict__ sc, const uint32_t *__restrict__ chunk_scene,
                                                 uint64_t nchunks, const uint32_t *__restrict__ rows,
-                                                const TriRec *__restrict__ recs, const uint4 *__restrict__ cov,
+                                                const uint4 *__restrict__ bbox, const uint4 *__restrict__ cov,
                                                 const SceneStats *__restrict__ stats,
                                                 const uint32_t *__restrict__ strip_off, uint32_t *__restrict__ strip_fill,
                                                 uint2 *__restrict__ entries, uint32_t strip_mode) {
@@ -1425,7 +1429,7 @@ __global__ void __launch_bounds__(kBlock) k_bin(const SceneDev *__restrict__ sc,
         const uint32_t h = s.strip_h;
         uint32_t by0 = 0, by1 = 0, q0 = 0, nst = 0;
         if (rows[t] & kRowsBinned) {
-            const uint4 w3 = __ldg(reinterpret_cast<const uint4 *>(recs + t) + 3);  // bx0, bx1, by0, by1
+            const uint4 w3 = __ldg(bbox + t);  // bx0, bx1, by0, by1
             by0 = w3.z;
             by1 = w3.w;
             q0 = by0 / h;
