@@ -278,6 +278,8 @@ int plan_scene(const euc_scene &sc, Plan &p) {
     }
     s.W = W;
     s.H = H;
+    s.ndc_x = 2.0f / (float)W;
+    s.ndc_y = -2.0f / (float)H;
     s.gr = (uint32_t)gr;
     s.level = level;
     s.ppitch = px_empty ? 0 : (px.pitch ? px.pitch : px.width * fmt_bpp(px.format));
@@ -1071,7 +1073,7 @@ void graph_free(euc_graph *g) {
 // ---------------------------------------------------------------------------
 constexpr size_t kShapeCap = 512;  // recorded shapes of a context at most (least recently used go)
 constexpr size_t kSightCap = 4096; // shapes counted before the count starts over
-constexpr size_t kStageParamBytes = 1008;  // one scene's table, bases and uniforms (at most 240 + 64 + 512)
+constexpr size_t kStageParamBytes = 1008;  // one scene's table, bases and uniforms (at most 256 + 64 + 512)
 
 struct alignas(16) StageParam {
     uint32_t n, pad[3];                  // bytes of b to write (a multiple of 16)

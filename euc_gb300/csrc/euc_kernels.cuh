@@ -125,6 +125,9 @@ struct SceneDev {
     // strip_h, global strips strip_base .. strip_base + nstrips - 1
     uint32_t strip_h;
     uint32_t strip_base, nstrips;
+    // 2 / W and -2 / H, divided once by the host (IEEE, as every setup
+    // thread would): the NDC-to-screen matrix of triangles.rs:86-102
+    float ndc_x, ndc_y;
 };
 
 // Per-primitive record written by k_setup (128 bytes, 16-byte aligned).
@@ -695,7 +698,7 @@ __global__ void __launch_bounds__(kBlock) k_setup(const SceneDev *__restrict__ s
                     uint32_t tv = vid[0]; vid[0] = vid[2]; vid[2] = tv;
                 }
                 const float size_x = (float)s.W, size_y = (float)s.H;
-                const float nd[3][3] = {{2.0f / size_x, 0.0f, -1.0f}, {0.0f, -2.0f / size_y, 1.0f}, {0.0f, 0.0f, 1.0f}};
+                const float nd[3][3] = {{s.ndc_x, 0.0f, -1.0f}, {0.0f, s.ndc_y, 1.0f}, {0.0f, 0.0f, 1.0f}};
                 // coords_to_weights (triangles.rs:86-102)
                 const float A[3] = {h[0][0], h[0][1], h[0][3]};
                 const float B[3] = {h[1][0], h[1][1], h[1][3]};
@@ -2166,7 +2169,8 @@ EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, cons
 // [s_begin, s_end); rbase (global scene index, from plan_chunks) holds the first
 // chunk of each.
 template <class F>
-__global__ void __launch_bounds__(kBlock, 4) k_resolve(const SceneDev *__restrict__ sc, const uint64_t *__restrict__ rbase,
+__global__ void __launch_bounds__(kBlock, F::kResolveBlocks) k_resolve(const SceneDev *__restrict__ sc,
+                                                                    const uint64_t *__restrict__ rbase,
                                                     int s_begin, int s_end, uint32_t group,
                                                     const TriRec *__restrict__ recs, const float *__restrict__ vdata,
                                                     const unsigned long long *__restrict__ vbuf,
