@@ -946,6 +946,28 @@ __host__ __device__ inline uint64_t rect_area(const uint4 &c) {
 // is spent on pixels that no primitive reaches.
 constexpr int kChunkGroup = 16;
 
+// Entries i0, i0 + kBlock, i0 + 2 kBlock, ... of a row-major rectangle rw
+// wide, as (column, row): one division for the first entry and one for the
+// step, then a fixed quotient and remainder per step (the column wraps at
+// most once, since both it and the remainder are below rw).
+struct RectWalk {
+    uint32_t rx, ry, qs, rs, rw;
+    EUC_DEV RectWalk(uint32_t i0, uint32_t w) : rw(w) {
+        ry = i0 / w;
+        rx = i0 - ry * w;
+        qs = (uint32_t)kBlock / w;
+        rs = (uint32_t)kBlock - qs * w;
+    }
+    EUC_DEV void next() {
+        rx += rs;
+        ry += qs;
+        if (rx >= rw) {
+            rx -= rw;
+            ++ry;
+        }
+    }
+};
+
 // Each thread of k_init initialises kInitPer entries of the covered rectangle,
 // kBlock apart, so that every load and store instruction of a warp covers 32
 // consecutive entries and the kInitPer depth loads are in flight together; a
@@ -990,14 +1012,14 @@ __global__ void __launch_bounds__(kBlock) k_init(const SceneDev *__restrict__ sc
             const uint4 cv = cov[si];
             const uint32_t area = (uint32_t)rect_area(cv);
             if (i0 >= area) continue;
-            const uint32_t rw = ~cv.z - cv.x;
+            RectWalk rk(i0, ~cv.z - cv.x);
             uint32_t px[kInitPer];
             float d[kInitPer];
 #pragma unroll
-            for (int k = 0; k < kInitPer; ++k) {
+            for (int k = 0; k < kInitPer; ++k, rk.next()) {
                 const uint32_t i = i0 + k * kBlock;
                 const bool live = i < area;
-                const uint32_t ry = i / rw, x = cv.x + (i - ry * rw), y = cv.y + ry;
+                const uint32_t x = cv.x + rk.rx, y = cv.y + rk.ry;
                 px[k] = live ? y * s.W + x : 0xFFFFFFFFu;
                 d[k] = (live && s.keytype == KEY_MIN)
                            ? *reinterpret_cast<const float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x)
@@ -1997,16 +2019,16 @@ struct ResolveSmem {
 template <class F>
 EUC_DEV void resolve_direct_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, const TriRec *__restrict__ recs,
                                   const float *__restrict__ vdata, const unsigned long long *__restrict__ vbuf) {
-    const uint32_t rw = ~cv.z - cv.x, area = (uint32_t)rect_area(cv);  // pixel indices fit 32 bits
+    const uint32_t area = (uint32_t)rect_area(cv);  // pixel indices fit 32 bits
     const uint32_t i0 = (uint32_t)lb * (kBlock * kDirectPer) + threadIdx.x;
+    RectWalk rk(i0, ~cv.z - cv.x);
     uint32_t px[kDirectPer], py[kDirectPer];
     unsigned long long key[kDirectPer];
 #pragma unroll
-    for (int k = 0; k < kDirectPer; ++k) {
+    for (int k = 0; k < kDirectPer; ++k, rk.next()) {
         const uint32_t i = i0 + k * kBlock;
-        const uint32_t ry = i / rw;
-        px[k] = cv.x + (i - ry * rw);
-        py[k] = i < area ? cv.y + ry : 0xFFFFFFFFu;
+        px[k] = cv.x + rk.rx;
+        py[k] = i < area ? cv.y + rk.ry : 0xFFFFFFFFu;
         key[k] = i < area ? vbuf[s.pix_base + (uint64_t)py[k] * s.W + px[k]] : 0ull;
     }
     // unrolled: the record and varyings gathers of the pixels overlap
