@@ -2063,9 +2063,12 @@ EUC_DEV bool chunk_pixel(const SceneDev &s, const uint4 &cv, uint64_t lb, bool q
         const uint32_t p0 = pair_of_row(cv.y, s.gr), a0 = cv.x >> 4;
         const uint32_t cols = ((~cv.z - 1) >> 4) - a0 + 1;
         const uint64_t npairs = pair_of_row(~cv.w - 1, s.gr) - p0 + 1;
-        const uint64_t w = lb * (kBlock / 32) + (tid >> 5);
-        if (w >= npairs * cols) return false;
-        const uint32_t p = p0 + (uint32_t)(w / cols), a = a0 + (uint32_t)(w % cols);
+        const uint64_t w64 = lb * (kBlock / 32) + (tid >> 5);
+        if (w64 >= npairs * cols) return false;
+        // a scene has fewer than 2^32 / 32 tiles (its pixel indices fit 32
+        // bits): a 32-bit division, not a 64-bit one
+        const uint32_t w = (uint32_t)w64, wr = w / cols;
+        const uint32_t p = p0 + wr, a = a0 + (w - wr * cols);
         const uint32_t b = p / ppb, k = p % ppb;
         lo = b * s.gr;
         x = a * 16 + (lane & 15);
