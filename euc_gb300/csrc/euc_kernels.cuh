@@ -2003,10 +2003,19 @@ __global__ void __launch_bounds__(kBlock) k_prep(const PrepArgs prep) {
     if (i < prep.n) prep_clear(prep, i);
 }
 
+// The per-scene part of chunk_pixel's mapping (what it divides by the band
+// height), computed when a block's chunks reach a new scene.
+struct ChunkGeom {
+    bool quads;                  // resolve_by_quads: 16x2-pixel tiles
+    uint32_t p0, a0, cols, ppb;  // first row pair and tile column, tile columns, row pairs per band
+    uint64_t ntiles;             // tiles of the covered rectangle
+};
+
 // One warp's job list in k_resolve: its 32 pixels' winners and positions,
 // their fragment evaluations and the results.
 template <class F>
 struct ResolveSmem {
+    ChunkGeom geo;  // of the warp's current scene (kept here, not in registers)
     uint32_t t[32];
     uint32_t xy[32][3];
     uint16_t job[4 * 32];
@@ -2054,22 +2063,29 @@ EUC_DEV void resolve_direct_chunk(const SceneDev &s, const uint4 &cv, uint64_t l
 
 // This thread's pixel in chunk lb of a scene's covered rectangle (which is
 // not empty, or the scene would have no chunks) and the first row of its band.
-EUC_DEV bool chunk_pixel(const SceneDev &s, const uint4 &cv, uint64_t lb, bool quads, uint32_t &x, uint32_t &y,
-                         uint32_t &lo) {
+EUC_DEV ChunkGeom chunk_geom(const SceneDev &s, const uint4 &cv) {
+    ChunkGeom g;
+    g.quads = resolve_by_quads(s);
+    g.ppb = (s.gr + 1) >> 1;
+    g.a0 = cv.x >> 4;
+    g.cols = ((~cv.z - 1) >> 4) - g.a0 + 1;
+    g.p0 = g.quads ? pair_of_row(cv.y, s.gr) : 0u;
+    g.ntiles = g.quads ? (uint64_t)(pair_of_row(~cv.w - 1, s.gr) - g.p0 + 1) * g.cols : 0ull;
+    return g;
+}
+
+EUC_DEV bool chunk_pixel(const SceneDev &s, const uint4 &cv, const ChunkGeom &g, uint64_t lb, uint32_t &x,
+                         uint32_t &y, uint32_t &lo) {
     const int tid = threadIdx.x, lane = tid & 31;
     x = y = lo = 0;
-    if (quads) {  // warp = 16x2 pixels on whole 2x2 cells of the band-relative grid
-        const uint32_t ppb = (s.gr + 1) >> 1;
-        const uint32_t p0 = pair_of_row(cv.y, s.gr), a0 = cv.x >> 4;
-        const uint32_t cols = ((~cv.z - 1) >> 4) - a0 + 1;
-        const uint64_t npairs = pair_of_row(~cv.w - 1, s.gr) - p0 + 1;
+    if (g.quads) {  // warp = 16x2 pixels on whole 2x2 cells of the band-relative grid
         const uint64_t w64 = lb * (kBlock / 32) + (tid >> 5);
-        if (w64 >= npairs * cols) return false;
+        if (w64 >= g.ntiles) return false;
         // a scene has fewer than 2^32 / 32 tiles (its pixel indices fit 32
         // bits): a 32-bit division, not a 64-bit one
-        const uint32_t w = (uint32_t)w64, wr = w / cols;
-        const uint32_t p = p0 + wr, a = a0 + (w - wr * cols);
-        const uint32_t b = p / ppb, k = p % ppb;
+        const uint32_t w = (uint32_t)w64, wr = w / g.cols;
+        const uint32_t p = g.p0 + wr, a = g.a0 + (w - wr * g.cols);
+        const uint32_t b = p / g.ppb, k = p - b * g.ppb;
         lo = b * s.gr;
         x = a * 16 + (lane & 15);
         y = lo + 2 * k + (lane >> 4);
@@ -2087,14 +2103,15 @@ EUC_DEV bool chunk_pixel(const SceneDev &s, const uint4 &cv, uint64_t lb, bool q
 
 // One 256-pixel chunk `lb` of scene `s`; every thread of the block calls it.
 template <class F>
-EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, uint64_t lb, const TriRec *__restrict__ recs,
+EUC_DEV void resolve_chunk(const SceneDev &s, const uint4 &cv, const ChunkGeom &geo, uint64_t lb,
+                           const TriRec *__restrict__ recs,
                            const float *__restrict__ vdata, const unsigned long long *__restrict__ vbuf,
                            ResolveSmem<F> &sm) {
     const int lane = threadIdx.x & 31;
     // 1. this thread's pixel
     uint32_t x, y, lo;
-    const bool quads = resolve_by_quads(s);
-    const bool inside = chunk_pixel(s, cv, lb, quads, x, y, lo);
+    const bool quads = geo.quads;
+    const bool inside = chunk_pixel(s, cv, geo, lb, x, y, lo);
     uint32_t t = 0xFFFFFFFFu;
     float z = 0.0f;
     const bool win = inside && decode_key(s, vbuf[s.pix_base + (uint64_t)y * s.W + x], t, z);
@@ -2208,7 +2225,8 @@ __global__ void __launch_bounds__(kBlock, F::kResolveBlocks) k_resolve(const Sce
     const uint64_t c_begin = base[0], c_end = base[n];
     for (uint64_t g = blockIdx.x; c_begin + g * group < c_end; g += gridDim.x) {
         const uint64_t c0 = c_begin + g * group;
-        int si = find_scene(base, n, c0);
+        int si = find_scene(base, n, c0), gsi = -1;
+        const ChunkGeom &geo = sm.geo;
         for (uint64_t c = c0; c < c0 + group && c < c_end; ++c) {
             si = advance_scene(base, n, si, c);
             const SceneDev &s = sc[s_begin + si];
@@ -2216,15 +2234,20 @@ __global__ void __launch_bounds__(kBlock, F::kResolveBlocks) k_resolve(const Sce
                 resolve_direct_chunk<F>(s, cov[s_begin + si], c - base[si], recs, vdata, vbuf);
             } else {
                 const uint4 cv = cov[s_begin + si];
+                if (si != gsi) {  // the block's chunks reached a new scene
+                    if ((threadIdx.x & 31) == 0) sm.geo = chunk_geom(s, cv);
+                    __syncwarp();
+                    gsi = si;
+                }
                 // the keys of this block's next chunk in the same scene start
                 // on their way to L2 (the keys of a large batch outgrow it)
                 const uint64_t nc = c + 1 < c0 + group ? c + 1 : c_begin + (g + gridDim.x) * group;
                 if (nc < base[si + 1]) {
                     uint32_t px, py, plo;
-                    if (chunk_pixel(s, cv, nc - base[si], resolve_by_quads(s), px, py, plo))
+                    if (chunk_pixel(s, cv, geo, nc - base[si], px, py, plo))
                         asm volatile("prefetch.global.L2 [%0];" ::"l"(vbuf + s.pix_base + (uint64_t)py * s.W + px));
                 }
-                resolve_chunk<F>(s, cv, c - base[si], recs, vdata, vbuf, sm);
+                resolve_chunk<F>(s, cv, geo, c - base[si], recs, vdata, vbuf, sm);
                 __syncwarp();  // the next chunk reuses the warp's shared memory
             }
         }
