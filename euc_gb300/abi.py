@@ -38,7 +38,7 @@ HOST_COPY_AUTO, HOST_COPY_STAGED, HOST_COPY_DIRECT = 0, 1, 2
 CULL_NONE, CULL_BACK, CULL_FRONT = 0, 1, 2
 Y_DOWN, Y_UP = 0, 1
 LEFT, RIGHT = 0, 1
-FMT_NONE, FMT_RGBA8, FMT_BGRA8, FMT_RGB8, FMT_R32F = 0, 1, 2, 3, 4
+FMT_NONE, FMT_RGBA8, FMT_BGRA8, FMT_RGB8, FMT_R32F, FMT_RGBA32F = 0, 1, 2, 3, 4, 5
 SHADER_FLAT, SHADER_VCOLOR, SHADER_GOURAUD, SHADER_TEXTURED, SHADER_PHONG, SHADER_SHADOW = range(6)
 BLEND_REPLACE, BLEND_ALPHA = 0, 1
 FILTER_NEAREST, FILTER_LINEAR = 0, 1
@@ -51,7 +51,7 @@ FLAG_ORDERED = 2
 STAGE_NAMES = ("vertex", "setup", "scan", "init", "raster", "resolve")
 STAGE_COUNT = len(STAGE_NAMES)
 
-FMT_BPP = {FMT_NONE: 0, FMT_RGBA8: 4, FMT_BGRA8: 4, FMT_RGB8: 3, FMT_R32F: 4}
+FMT_BPP = {FMT_NONE: 0, FMT_RGBA8: 4, FMT_BGRA8: 4, FMT_RGB8: 3, FMT_R32F: 4, FMT_RGBA32F: 16}
 
 
 class PipelineDesc(C.Structure):

@@ -112,6 +112,7 @@ uint32_t fmt_bpp(uint32_t f) {
     switch (f) {
     case EUC_FMT_RGBA8: case EUC_FMT_BGRA8: case EUC_FMT_R32F: return 4;
     case EUC_FMT_RGB8: return 3;
+    case EUC_FMT_RGBA32F: return 16;
     default: return 0;
     }
 }
@@ -211,7 +212,7 @@ int plan_scene(const euc_scene &sc, Plan &p) {
         if (bpp == 0 || px.format == EUC_FMT_R32F) return EUC_ERR_INVALID;
         const uint32_t pitch = px.pitch ? px.pitch : px.width * bpp;
         if (pitch < px.width * bpp) return EUC_ERR_INVALID;
-        if (bpp == 4 && ((pitch & 3) || ((uintptr_t)px.data & 3))) return EUC_ERR_INVALID;
+        if (bpp % 4 == 0 && ((pitch & 3) || ((uintptr_t)px.data & 3))) return EUC_ERR_INVALID;
     }
     if (!dp_empty && uses_depth) {
         if (dp.format != EUC_FMT_R32F) return EUC_ERR_INVALID;

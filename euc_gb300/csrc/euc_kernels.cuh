@@ -1818,8 +1818,16 @@ template <class F>
 EUC_DEV void store_pixel(const SceneDev &s, uint32_t x, uint32_t y, const float *frag) {
     const float c0 = frag[0], c1 = F::NF > 1 ? frag[F::NF > 1 ? 1 : 0] : 0.0f;
     const float c2 = F::NF > 2 ? frag[F::NF > 2 ? 2 : 0] : 0.0f, c3 = F::NF > 3 ? frag[F::NF > 3 ? 3 : 0] : 0.0f;
-    const uint32_t r8 = sat_u8(F::pack(c0)), g8 = sat_u8(F::pack(c1)), b8 = sat_u8(F::pack(c2)), a8 = sat_u8(F::pack(c3));
     uint8_t *p = s.pixel + (uint64_t)y * s.ppitch;
+    if (s.pfmt == EUC_FMT_RGBA32F) {  // the fragment as it is (no pack)
+        float *q = reinterpret_cast<float *>(p) + 4ull * x;
+        q[0] = c0;
+        q[1] = c1;
+        q[2] = c2;
+        q[3] = c3;
+        return;
+    }
+    const uint32_t r8 = sat_u8(F::pack(c0)), g8 = sat_u8(F::pack(c1)), b8 = sat_u8(F::pack(c2)), a8 = sat_u8(F::pack(c3));
     if (s.pfmt == EUC_FMT_RGBA8) {
         reinterpret_cast<uint32_t *>(p)[x] = r8 | (g8 << 8) | (b8 << 16) | (a8 << 24);
     } else if (s.pfmt == EUC_FMT_BGRA8) {
@@ -2462,14 +2470,22 @@ __global__ void __launch_bounds__(kBlock) k_resolve_ordered(const SceneDev *__re
     const uint32_t off = (uint32_t)e, n = (uint32_t)(e >> 32);
     if (n == 0) return;
     float *dp = s.depth ? reinterpret_cast<float *>(s.depth + (uint64_t)y * s.dpitch + 4ull * x) : nullptr;
-    uint8_t *pp = s.pixel ? s.pixel + (uint64_t)y * s.ppitch + (uint64_t)x * (s.pfmt == EUC_FMT_RGB8 ? 3u : 4u) : nullptr;
+    const bool f32 = s.pfmt == EUC_FMT_RGBA32F;  // the pixel kept as four floats
+    uint8_t *pp = s.pixel ? s.pixel + (uint64_t)y * s.ppitch +
+                                (uint64_t)x * (f32 ? 16u : s.pfmt == EUC_FMT_RGB8 ? 3u : 4u)
+                          : nullptr;
     const bool uses_depth = s.depth_test != EUC_TEST_NONE || s.depth_write;
     float D = uses_depth ? *dp : 0.0f;
     const int ri = s.pfmt == EUC_FMT_BGRA8 ? 2 : 0, bi = s.pfmt == EUC_FMT_BGRA8 ? 0 : 2;
     const int nch = s.pfmt == EUC_FMT_RGB8 ? 3 : 4;
     uint32_t ch[4] = {0, 0, 0, 255};
-    if (s.pixel_write)
-        for (int i = 0; i < nch; ++i) ch[i] = pp[i];
+    float pf[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (s.pixel_write) {
+        if (f32)
+            for (int i = 0; i < 4; ++i) pf[i] = reinterpret_cast<const float *>(pp)[i];
+        else
+            for (int i = 0; i < nch; ++i) ch[i] = pp[i];
+    }
     const typename F::U &u = *reinterpret_cast<const typename F::U *>(s.uniforms);
     const float *vb = vdata + (s.geom ? s.gvd_base : s.vd_base);
     uint32_t last = 0;  // 1 + the primitive processed last
@@ -2497,11 +2513,22 @@ __global__ void __launch_bounds__(kBlock) k_resolve_ordered(const SceneDev *__re
         float c[4] = {frag[0], F::NF > 1 ? frag[F::NF > 1 ? 1 : 0] : 0.0f, F::NF > 2 ? frag[F::NF > 2 ? 2 : 0] : 0.0f,
                       F::NF > 3 ? frag[F::NF > 3 ? 3 : 0] : 0.0f};
         if (s.blend == EUC_BLEND_ALPHA) {  // src-over on the unpacked old pixel
-            const float old[4] = {(float)ch[ri] / 255.0f, (float)ch[1] / 255.0f, (float)ch[bi] / 255.0f,
-                                  nch == 3 ? 1.0f : (float)ch[3] / 255.0f};
+            float old[4];
+            if (f32) {
+                for (int i = 0; i < 4; ++i) old[i] = pf[i];
+            } else {
+                old[0] = (float)ch[ri] / 255.0f;
+                old[1] = (float)ch[1] / 255.0f;
+                old[2] = (float)ch[bi] / 255.0f;
+                old[3] = nch == 3 ? 1.0f : (float)ch[3] / 255.0f;
+            }
             const float a = c[3];
 #pragma unroll
             for (int i = 0; i < 4; ++i) c[i] = c[i] * a + old[i] * (1.0f - a);
+        }
+        if (f32) {
+            for (int i = 0; i < 4; ++i) pf[i] = c[i];
+            continue;
         }
         ch[ri] = sat_u8(F::pack(c[0]));
         ch[1] = sat_u8(F::pack(c[1]));
@@ -2509,8 +2536,12 @@ __global__ void __launch_bounds__(kBlock) k_resolve_ordered(const SceneDev *__re
         if (nch == 4) ch[3] = sat_u8(F::pack(c[3]));
     }
     if (s.depth_write) *dp = D;
-    if (s.pixel_write)
-        for (int i = 0; i < nch; ++i) pp[i] = (uint8_t)ch[i];
+    if (s.pixel_write) {
+        if (f32)
+            for (int i = 0; i < 4; ++i) reinterpret_cast<float *>(pp)[i] = pf[i];
+        else
+            for (int i = 0; i < nch; ++i) pp[i] = (uint8_t)ch[i];
+    }
 }
 
 }  // namespace eucg

@@ -54,6 +54,8 @@ class DeviceFrame:
         for t in frame.targets:
             if t.fmt == abi.FMT_R32F:
                 self.targets[t.name] = torch.empty((t.height, t.width), dtype=torch.float32, device=self.device)
+            elif t.fmt == abi.FMT_RGBA32F:
+                self.targets[t.name] = torch.empty((t.height, t.width, 4), dtype=torch.float32, device=self.device)
             else:
                 self.targets[t.name] = torch.empty((t.height, t.width, t.bpp), dtype=torch.uint8, device=self.device)
         self._clear_px = {t.name: torch.from_numpy(t.host_alloc()[:1, :1].copy()).to(self.device)
@@ -147,7 +149,10 @@ class DeviceBatch:
                 else:
                     co = (co + 15) & ~15
                     n = t.width * t.height * t.bpp
-                    df.targets[t.name] = self.color[co:co + n].view(t.height, t.width, t.bpp)
+                    view = self.color[co:co + n].view(t.height, t.width, t.bpp)
+                    if t.fmt == abi.FMT_RGBA32F:  # four floats a pixel (the offset is 16-byte aligned)
+                        view = view.view(torch.float32)
+                    df.targets[t.name] = view
                     co += n
             df._clear_px = {}
             self.frames.append(df)

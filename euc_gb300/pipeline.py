@@ -122,6 +122,9 @@ class Buffer2d:
             fmt = abi.FMT_R32F if isinstance(value, float) else abi.FMT_RGBA8
         if fmt == abi.FMT_R32F:
             arr = np.full((h, w), np.float32(value), dtype=np.float32)
+        elif fmt == abi.FMT_RGBA32F:  # Buffer2d<[f32; 4]>: value is a float or four floats
+            arr = np.empty((h, w, 4), dtype=np.float32)
+            arr[...] = np.asarray(value, dtype=np.float32)
         else:
             bpp = abi.FMT_BPP[fmt]
             px = np.frombuffer(int(value).to_bytes(8, "little")[:bpp], dtype=np.uint8)
@@ -141,6 +144,13 @@ class Buffer2d:
     def clear(self, value):
         if self.fmt == abi.FMT_R32F:
             self.data[...] = float(np.float32(value))
+        elif self.fmt == abi.FMT_RGBA32F:
+            px = np.asarray(value, dtype=np.float32) * np.ones(4, dtype=np.float32)
+            if self.on_device:
+                import torch
+                self.data.copy_(torch.from_numpy(px).to(self.data.device).expand_as(self.data))
+            else:
+                self.data[...] = px
         else:
             bpp = abi.FMT_BPP[self.fmt]
             px = np.frombuffer(int(value).to_bytes(8, "little")[:bpp], dtype=np.uint8)

@@ -33,7 +33,7 @@ class TargetSpec:
     width: int
     height: int
     fmt: int
-    clear: object  # int (packed little-endian pixel) or float (depth)
+    clear: object  # int (packed little-endian pixel), float (depth), float or 4 floats (RGBA32F)
 
     @property
     def bpp(self):
@@ -42,6 +42,10 @@ class TargetSpec:
     def host_alloc(self):
         if self.fmt == abi.FMT_R32F:
             return np.full((self.height, self.width), np.float32(self.clear), dtype=np.float32)
+        if self.fmt == abi.FMT_RGBA32F:  # four floats a pixel
+            arr = np.empty((self.height, self.width, 4), dtype=np.float32)
+            arr[...] = np.asarray(self.clear, dtype=np.float32)
+            return arr
         px = np.frombuffer(int(self.clear).to_bytes(8, "little")[: self.bpp], dtype=np.uint8)
         return np.ascontiguousarray(np.broadcast_to(px, (self.height, self.width, self.bpp)))
 

@@ -67,7 +67,12 @@ enum euc_format {
     EUC_FMT_RGBA8 = 1, /* bytes r,g,b,a                                       */
     EUC_FMT_BGRA8 = 2, /* bytes b,g,r,a (u32::from_le_bytes of Rgba(b,g,r,a)) */
     EUC_FMT_RGB8 = 3,  /* bytes r,g,b                                         */
-    EUC_FMT_R32F = 4   /* f32                                                  */
+    EUC_FMT_R32F = 4,  /* f32                                                  */
+    /* f32 r,g,b,a: a colour target that keeps the fragment as it is, as a
+     * Buffer2d<[f32; 4]> (or Rgba<f32>) pixel type does: REPLACE stores the
+     * fragment's four values (no pack, no saturation), ALPHA is src-over on
+     * the stored floats.  Colour targets only (not a texture format).       */
+    EUC_FMT_RGBA32F = 5
 };
 
 /* Source layouts for texture ingest: the image crate's 8-bit pixel types

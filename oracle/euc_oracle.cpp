@@ -396,6 +396,7 @@ inline uint32_t fmt_bpp(uint32_t f) {
     switch (f) {
     case EUC_FMT_RGBA8: case EUC_FMT_BGRA8: case EUC_FMT_R32F: return 4;
     case EUC_FMT_RGB8: return 3;
+    case EUC_FMT_RGBA32F: return 16;
     default: return 0;
     }
 }
@@ -426,6 +427,16 @@ struct Target {
 template <class S>
 void blend_pixel(const S &sh, uint32_t blend, uint8_t *px, uint32_t fmt, const float *f) {
     float c[4] = {f[0], S::NF > 1 ? f[1] : 0.0f, S::NF > 2 ? f[2] : 0.0f, S::NF > 3 ? f[3] : 0.0f};
+    if (fmt == EUC_FMT_RGBA32F) {  // a float pixel keeps the fragment: no pack, src-over on the floats
+        if (blend == EUC_BLEND_ALPHA) {
+            float old[4];
+            std::memcpy(old, px, sizeof(old));
+            const float a = c[3];
+            for (int i = 0; i < 4; ++i) c[i] = c[i] * a + old[i] * (1.0f - a);
+        }
+        std::memcpy(px, c, sizeof(c));
+        return;
+    }
     int ri = 0, gi = 1, bi = 2, ai = 3;
     if (fmt == EUC_FMT_BGRA8) { ri = 2; bi = 0; }
     if (blend == EUC_BLEND_ALPHA) {

@@ -37,12 +37,21 @@ def run_gpu(ctx, frame, device="cuda:0"):
 
 
 def assert_targets_match(frame, ref, got, color_tol=0):
-    """Depth bit-exact; colour exact or within color_tol per 8-bit channel;
-    the set of written colour pixels identical."""
+    """Depth bit-exact; colour exact or within color_tol per 8-bit channel
+    (an f32 colour target: bit-exact, or within a relative 1e-5 where
+    color_tol allows a step); the set of written colour pixels identical."""
     for t in frame.targets:
         a, b = ref[t.name], got[t.name]
         assert a.shape == b.shape, t.name
-        if t.fmt == abi.FMT_R32F:
+        if t.fmt == abi.FMT_RGBA32F:
+            if color_tol == 0:
+                ai, bi = a.view(np.uint32), b.view(np.uint32)
+                bad = np.argwhere(ai != bi)
+            else:
+                bad = np.argwhere(~np.isclose(a, b, rtol=1e-5, atol=1e-6))
+            assert bad.size == 0, "%s: %d f32 channels differ, first at %s: %r vs %r" % (
+                t.name, len(bad), bad[0].tolist(), a[tuple(bad[0][:2])], b[tuple(bad[0][:2])])
+        elif t.fmt == abi.FMT_R32F:
             ai, bi = a.view(np.uint32), b.view(np.uint32)
             bad = np.argwhere(ai != bi)
             assert bad.size == 0, "%s: %d depth words differ, first at %s: %r vs %r" % (

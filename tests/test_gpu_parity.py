@@ -42,6 +42,16 @@ def _fmt(make, fmt):
     return wrapped
 
 
+def _f32(make, clear=(0.25, 0.5, 0.75, 1.0)):
+    """The colour target as four floats a pixel (Buffer2d<[f32; 4]>)."""
+    def wrapped():
+        f = make()
+        t = f.target("color")
+        f.targets[f.targets.index(t)] = scenes.TargetSpec("color", t.width, t.height, abi.FMT_RGBA32F, clear)
+        return f
+    return wrapped
+
+
 def _clear(make, name, value):
     def wrapped():
         f = make()
@@ -168,6 +178,13 @@ CASES = {
     "tex_nearest_mirror": (_textured(abi.FILTER_NEAREST, abi.WRAP_MIRROR), 0),
     "tex_nearest_none": (_textured(abi.FILTER_NEAREST, abi.WRAP_NONE), 0),
     "flat": (_flat(), 0),
+    "f32_sphere": (_f32(_sphere(seed=3)), 0),
+    "f32_flat": (_f32(_flat()), 0),
+    "f32_tex_linear_tile": (_f32(_textured(abi.FILTER_LINEAR, abi.WRAP_TILE)), 0),
+    "f32_soup_less": (_f32(_soup(seed=2)), 0),
+    "f32_alpha_soup": (_f32(_soup(seed=21, alpha=True)), 0),
+    "f32_alpha_soup_msaa1": (_f32(_soup(seed=24, alpha=True, aa_level=1)), 0),
+    "f32_knot_aa1": (_f32(_knot(1)), 1),
     "unindexed": (_unindexed(), 0),
     # order-dependent blend: per-pixel fragment lists replayed in order
     "alpha_soup_less": (_soup(seed=21, alpha=True), 0),
