@@ -2,7 +2,9 @@
 
 Bar: depth bit-exact, per-pass candidate-fragment counts exact, colour exact
 for shaders without transcendental functions and within +-1 LSB per 8-bit
-channel for the Phong shader (powf differs by ulps between libm and CUDA).
+channel for the Phong shader (its lighting uses the hardware reciprocal square
+root and power; texel and shadow-map coordinates stay exact); on an f32 colour
+target Phong within a relative 1e-5, the others bit-exact.
 """
 import ctypes as C
 
