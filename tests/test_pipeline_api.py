@@ -100,6 +100,20 @@ def test_buffer2d_fill_and_clear():
     assert Empty().size() == [0, 0]
 
 
+def test_buffer2d_f32_colour():
+    # Buffer2d<[f32; 4]>: four floats a pixel, 16 bytes, the pitch a row of them
+    b = Buffer2d.fill([5, 3], (0.25, 0.5, 0.75, 1.0), fmt=abi.FMT_RGBA32F)
+    assert b.size() == [5, 3] and b.data.dtype == np.float32 and b.data.shape == (3, 5, 4)
+    assert np.array_equal(b.data[2, 4], np.float32([0.25, 0.5, 0.75, 1.0]))
+    t = b.target()
+    assert (t.width, t.height, t.pitch, t.format) == (5, 3, 5 * 16, abi.FMT_RGBA32F)
+    b.clear(0.5)
+    assert (b.data == 0.5).all()
+    b.clear((1.0, 2.0, 3.0, 4.0))
+    assert np.array_equal(b.data[0, 0], np.float32([1.0, 2.0, 3.0, 4.0]))
+    assert abi.FMT_BPP[abi.FMT_RGBA32F] == 16
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("where", ["host", "device"])
 def test_render_matches_oracle(where):
