@@ -43,8 +43,7 @@ uint32_t bpp_of(uint32_t f) {
     switch (f) {
     case EUC_FMT_RGBA8: case EUC_FMT_BGRA8: case EUC_FMT_R32F: return 4;
     case EUC_FMT_RGB8: return 3;
-    case EUC_FMT_RGBA32F: return 16;
-    default: return 0;
+    default: return 0;  // f32 colour targets are not served (the fill writes 3- or 4-byte texels)
     }
 }
 

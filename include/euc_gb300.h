@@ -464,7 +464,7 @@ typedef struct euc_server_config {
 
 typedef struct euc_server_target {
     uint32_t width, height;
-    uint32_t format;   /* euc_format                                                   */
+    uint32_t format;   /* euc_format, not EUC_FMT_RGBA32F (rejected: EUC_ERR_INVALID)    */
     uint32_t clear;    /* colour: little-endian packed texel; R32F: the f32 bit pattern */
     uint32_t readback; /* non-zero: copied to the request's `out` on completion         */
     uint32_t reserved;
