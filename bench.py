@@ -36,6 +36,9 @@ Printed as one JSON line (rank 0):
 
 With --impl reference the CPU oracle is timed alone on the same workload (the
 reference's CPU path; euc itself is Rust and cannot be built here).
+The launch shape is autotuned per workload (strip path, raster and chunk
+knobs); --no-tune keeps the default shape and --tuning '{"strip_path": 2}'
+(fields of euc_tuning as JSON) fixes one, for profiles of a known shape.
 With torchrun (N > 1) every rank renders its own 256 scenes (replicas, no
 collective on the data path) and the slowest rank's time is used.
 """
